@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 muFFT FFT path.
+
+Headline (default): one forward c2c FFT of N = 2^24 complex64 points per step
+(the multi-pass configuration the metric "c2c GFLOP/s (5N log2 N) + % HBM
+roofline" is quoted on), through libmufft_gb300's C ABI:
+
+  value     GFLOP/s = 5 N log2 N / device time per step, inputs resident in HBM,
+            rotating over 4 input/output buffer sets of 256 MiB (larger than L2)
+  e2e       the same metric through mufft_execute_plan_1d() on pinned host
+            buffers: host->device copy, both kernels, device->host copy per step
+  roofline  the dominant kernel's algorithmic bytes per launch / its average
+            CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline  the reference's scalar C path (the oracle port, or the
+            reference itself where it was compiled) on all host cores, one
+            independent 2^24 transform per thread
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --workload c2c_4096x65536   (other shapes, one JSON line each)
+
+Multi-GPU (torchrun): every rank runs its own replica of the workload (the
+transform does not shard without an all-to-all); value = all ranks' flops /
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "c2c GFLOP/s (5N·log2N) + % HBM roofline; split-TC vs FP32 at equal FP64 error"
+
+# name -> (N, batch, description)
+WORKLOADS = {
+    "c2c_2^24": (1 << 24, 1, "c2c forward, N=2^24 complex64, one transform per step (four-step 4096 x 4096)"),
+    "c2c_4096x65536": (4096, 65536, "c2c forward, batch 65536 x N=4096 complex64 (single pass)"),
+    "c2c_1024x4096": (1024, 4096, "c2c forward, batch 4096 x N=1024 complex64 (single pass)"),
+}
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def committed_traffic(workload: str, kernel: str) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return float(json.loads(p.read_text())[workload][kernel]["bytes_per_launch"])
+    except (KeyError, ValueError, TypeError):
+        return None
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = b""
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.25)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self) -> dict | None:
+        if not self.out:
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in csv.reader(io.StringIO(self.out.decode(errors="replace"))):
+            if len(row) < 9:
+                continue
+            try:
+                sm.append(float(row[1]))
+                smax.append(float(row[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, row[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        # samples "under load" = the upper half of the clock samples window
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- distributed
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_baseline(N: int, batch: int, threads: int, rounds: int = 1, prefer_reference: bool = True) -> dict:
+    """Reference scalar path on host cores.  Each thread runs its own
+    transforms (muFFT plans are single-threaded, fft.c:60)."""
+    from mufft_gb300 import signals
+    from oracle.oracle import load_oracle, load_reference
+    ref = load_reference() if prefer_reference else None
+    kind = "reference" if ref is not None else "port"
+    x = signals.complex_uniform(2, N)
+    per_thread = max(1, min(batch, 8) if batch > 1 else 1)
+    flops = 5.0 * N * math.log2(N)
+    if ref is not None:
+        from mufft_gb300.capi import aligned_copy, aligned_zeros
+        xin = aligned_copy(x, np.complex64)
+        outs = [aligned_zeros(N, np.complex64) for _ in range(threads)]
+        plans = [ref.create_plan_1d_c2c(N, -1, 0) for _ in range(threads)]
+
+        def work(i):
+            for _ in range(per_thread * rounds):
+                ref.execute_plan_1d(plans[i], outs[i].ctypes.data, xin.ctypes.data)
+        ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+        t0 = time.perf_counter()
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        el = time.perf_counter() - t0
+        for p in plans:
+            ref.free_plan_1d(p)
+    else:
+        ora = load_oracle()
+        out = np.empty((threads, N), np.complex64)
+        plan = ora.create_plan_1d_c2c(N, -1, 0)
+        t0 = time.perf_counter()
+        for _ in range(per_thread * rounds):
+            # every thread transforms the same input into its own output row
+            ora.lib.oracle_execute_plan_1d_many(plan, out.ctypes.data, x.ctypes.data, threads, N * 8, 0, threads)
+        el = time.perf_counter() - t0
+        ora.free_plan_1d(plan)
+    total = flops * threads * per_thread * rounds
+    return {"value": total / el / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": kind,
+            "sample": f"{threads} threads x {per_thread * rounds} c2c N={N} forward transforms "
+                      f"({'reference muFFT, portable C tier' if kind == 'reference' and os.uname().machine != 'x86_64' else kind}), "
+                      f"{el:.2f} s wall", "seconds": el}
+
+
+# ------------------------------------------------------------------- ours
+
+def run_ours(args, world, rank, local, pg) -> dict | None:
+    import torch
+
+    import mufft_gb300
+    from mufft_gb300 import signals
+
+    torch.cuda.set_device(local)
+    lib = mufft_gb300.load()
+    N, B, desc = WORKLOADS[args.workload]
+    flops_step = 5.0 * N * math.log2(N) * B
+    algo_bytes_pass = 16.0 * N * B  # each pass reads and writes every point once (complex64)
+
+    plan = lib.gb_create_plan_1d_c2c_batched(N, -1, 0, B, 0, 0)
+    if not plan:
+        raise RuntimeError(lib.gb_last_error_string().decode())
+    launches = lib.gb_plan_1d_launches(plan)
+    elems = N * B
+    nsets = max(2, min(8, math.ceil(4 * 2 ** 30 / (16 * elems))))  # >= 4 GiB of rotating buffers
+    nsets = 4 if elems * 16 >= 2 ** 28 else nsets
+    x = signals.complex_uniform(2, elems)
+    xt = torch.from_numpy(x).cuda()
+    ins = [xt.clone() for _ in range(nsets)]
+    outs = [torch.empty_like(xt) for _ in range(nsets)]
+    del xt
+    st = torch.cuda.current_stream()
+    sp = st.cuda_stream
+
+    def step(i):
+        rc = lib.gb_execute_plan_1d_async(plan, outs[i % nsets].data_ptr(), ins[i % nsets].data_ptr(), sp)
+        if rc:
+            raise RuntimeError(lib.gb_last_error_string().decode())
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+
+    # accuracy of one output against FP64 (outside the timed region)
+    acc = None
+    if rank == 0 and N * B <= (1 << 24):
+        got = outs[(args.warmup - 1) % nsets].cpu().numpy().reshape(B, N)[: min(B, 64)]
+        ref = np.fft.fft(x.reshape(B, N)[: min(B, 64)].astype(np.complex128), axis=-1)
+        acc = {"rel_l2_vs_fp64": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+               "max_abs_vs_fp64": float(np.abs(got - ref).max())}
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(pg)
+        torch.cuda.synchronize()
+        ev0.record(st)
+        for i in range(args.steps):
+            step(args.warmup + i)
+        ev1.record(st)
+        torch.cuda.synchronize()
+        barrier(pg)
+    ms = ev0.elapsed_time(ev1)
+    ms_max = max_over_ranks(pg, ms)
+    ms_step = ms_max / args.steps
+
+    # per-kernel timing for the roofline (outside the headline region)
+    per_kernel = []
+    reps = max(5, args.steps)
+    for k in range(launches):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for i in range(reps):
+            rc = lib.gb_execute_plan_1d_launches_async(plan, outs[i % nsets].data_ptr(), ins[i % nsets].data_ptr(),
+                                                       k, 1, sp)
+            assert rc == 0
+        e1.record(st)
+        torch.cuda.synchronize()
+        per_kernel.append(e0.elapsed_time(e1) / reps)
+    import ctypes
+    dbuf = ctypes.create_string_buffer(4096)
+    lib.gb_plan_1d_describe(plan, dbuf, 4096)
+    kernels = dbuf.value.decode().split("; ")
+    dom = int(np.argmax(per_kernel))
+    peaks = load_peaks()
+    achieved = algo_bytes_pass / (per_kernel[dom] * 1e-3) / 1e9
+    traffic = committed_traffic(args.workload, f"launch{dom}")
+
+    # end to end through the fft.h API with pinned host buffers
+    e2e = None
+    if rank == 0 or world > 1:
+        nbytes = elems * 8
+        if B == 1:
+            hplan = lib.create_plan_1d_c2c(N, -1, 0)
+        else:
+            hplan = lib.gb_create_plan_1d_c2c_batched(N, -1, 0, B, 0, 0)
+        hin, hout = lib.alloc(nbytes), lib.alloc(nbytes)
+        ctypes.memmove(hin, x.ctypes.data, nbytes)
+        e2e_steps = max(3, min(args.steps, 10))
+        lib.execute_plan_1d(hplan, hout, hin)  # warm (staging buffers)
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            lib.execute_plan_1d(hplan, hout, hin)
+        el = time.perf_counter() - t0
+        lib.check("e2e execute")
+        el = max_over_ranks(pg, el)
+        lib.free(hin)
+        lib.free(hout)
+        lib.free_plan_1d(hplan)
+        e2e = {"value": world * flops_step * e2e_steps / el / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "ms_per_step": 1e3 * el / e2e_steps, "api": "mufft_execute_plan_1d (fft.h), pinned host buffers"}
+
+    lib.free_plan_1d(plan)
+    if rank != 0:
+        return None
+    res = {
+        "metric": METRIC,
+        "value": world * flops_step / (ms_step * 1e-3) / 1e9,
+        "unit": "GFLOP/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: complex64, re/im i.i.d. uniform [-1,1), SplitMix64 seed 2",
+        "config": {"workload": desc, "N": N, "batch": B, "parallelism": f"replicas x{world}",
+                   "l2": f"inputs larger than L2: {nsets} rotating input/output sets of {16 * elems / 2**20:.0f} MiB",
+                   "schedule": kernels},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                     "kernel": kernels[dom], "kernel_ms": per_kernel[dom],
+                     "algorithmic_bytes_per_launch": algo_bytes_pass,
+                     "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["source"] == "measured"
+                     else "fallback 6.8 TB/s",
+                     "per_kernel_ms": per_kernel,
+                     "frac_of_nominal_8tbs": achieved / 8000.0},
+        "e2e": e2e,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+        "accuracy": acc,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(N, B, threads=os.cpu_count() or 1)
+    return res
+
+
+def run_reference(args, world, rank, pg) -> dict | None:
+    if rank != 0:
+        return None
+    N, B, desc = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(N, B, threads)
+    samples = [cpu_baseline(N, B, threads) for _ in range(args.steps)]
+    secs = sum(s["seconds"] for s in samples)
+    value = statistics.mean(s["value"] for s in samples)
+    base = samples[0]
+    return {
+        "metric": METRIC, "impl": "reference", "value": value, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: complex64, re/im i.i.d. uniform [-1,1), SplitMix64 seed 2",
+        "config": {"workload": desc, "N": N, "batch": B, "parallelism": f"{threads} host threads"},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": base["kind"],
+                         "sample": base["sample"]},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c_2^24")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        res = run_reference(args, world, rank, pg)
+    else:
+        res = run_ours(args, world, rank, local, pg)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,104 @@
+/*
+ * mufft_gb300.h -- GB300 extensions to the muFFT C API.
+ *
+ * Nothing here has a counterpart in the reference, which is a single-threaded
+ * CPU library: these entry points expose what a GPU caller needs on top of
+ * fft.h -- batches, caller streams with device-resident buffers, error
+ * reporting (the reference's execute functions return void and cannot fail),
+ * and the GPU-only forms (ragged batched convolution, the convolution
+ * adjoint).  All functions are C ABI; pointers are plain addresses, streams
+ * are cudaStream_t passed as void*.
+ */
+#ifndef MUFFT_GB300_H__
+#define MUFFT_GB300_H__
+
+#include "fft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- errors */
+
+/* Error codes returned by the int-valued entry points and latched per thread
+ * by every entry point (the fft.h functions return void or NULL).  Positive
+ * values are cudaError_t codes from the CUDA runtime. */
+#define MUFFT_GB_OK 0
+#define MUFFT_GB_ERR_INVALID (-1)     /* bad size, flag, pointer or plan */
+#define MUFFT_GB_ERR_UNSUPPORTED (-2) /* valid for muFFT but not built here */
+#define MUFFT_GB_ERR_NO_DEVICE (-3)   /* no CUDA device visible */
+#define MUFFT_GB_ERR_HOST_POINTER (-4)/* async call given host memory */
+#define MUFFT_GB_ERR_ALLOC (-5)
+
+/* Last error of the calling thread (0 if none) and its text. */
+int mufft_gb_last_error(void);
+const char *mufft_gb_last_error_string(void);
+void mufft_gb_clear_error(void);
+
+/* ------------------------------------------------------------ batches */
+
+/* `batch` independent transforms per execute.  idist / odist: distance
+ * between consecutive transforms in elements of the input / output type
+ * (complex for c2c input and output, r2c output and c2r input; float for
+ * r2c input and c2r output).  0 selects the packed layout: c2c N (N/2 with
+ * MUFFT_FLAG_ZERO_PAD_UPPER_HALF) in and N out; r2c N (N/2) in and N/2+1
+ * (N with FULL_R2C) out; c2r N/2+1 in and N out.  Real distances must be
+ * even. */
+mufft_plan_1d *mufft_gb_create_plan_1d_c2c_batched(unsigned N, int direction, unsigned flags,
+                                                   unsigned batch, size_t idist, size_t odist);
+mufft_plan_1d *mufft_gb_create_plan_1d_r2c_batched(unsigned N, unsigned flags,
+                                                   unsigned batch, size_t idist, size_t odist);
+mufft_plan_1d *mufft_gb_create_plan_1d_c2r_batched(unsigned N, unsigned flags,
+                                                   unsigned batch, size_t idist, size_t odist);
+
+/* ------------------------------------------------- asynchronous execution */
+
+/* Enqueue on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ * without synchronising.  Buffers must be device-accessible (device or
+ * managed memory); host memory is rejected with MUFFT_GB_ERR_HOST_POINTER.
+ * A plan's scratch is reused by every execute, so two executes of one plan
+ * must not overlap on the GPU (enqueue them on one stream). */
+int mufft_gb_execute_plan_1d_async(mufft_plan_1d *plan, void *output, const void *input, void *stream);
+int mufft_gb_execute_plan_2d_async(mufft_plan_2d *plan, void *output, const void *input, void *stream);
+int mufft_gb_execute_conv_input_async(mufft_plan_conv *plan, unsigned block, void *output,
+                                      const void *input, void *stream);
+int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, const void *input_first,
+                                       const void *input_second, void *stream);
+
+/* Enqueue only launches [first, first + count) of a 1D plan's schedule (see
+ * mufft_gb_plan_1d_describe), for timing one kernel of a multi-pass plan.
+ * Intermediate launches read and write the plan's scratch. */
+int mufft_gb_execute_plan_1d_launches_async(mufft_plan_1d *plan, void *output, const void *input,
+                                            unsigned first, unsigned count, void *stream);
+
+/* ---------------------------------------------------------- introspection */
+
+/* Kernel launches one execute enqueues, and a one-line description of the
+ * GPU schedule (kernel, length, transforms per CTA, grid) into buf. */
+unsigned mufft_gb_plan_1d_launches(const mufft_plan_1d *plan);
+unsigned mufft_gb_plan_2d_launches(const mufft_plan_2d *plan);
+int mufft_gb_plan_1d_describe(const mufft_plan_1d *plan, char *buf, size_t size);
+int mufft_gb_plan_2d_describe(const mufft_plan_2d *plan, char *buf, size_t size);
+
+/* The same description for a 1D plan that would be built from these
+ * arguments, computed on the host without touching a GPU (kind: 0 c2c,
+ * 1 r2c, 2 c2r).  Returns MUFFT_GB_OK or the error plan creation would
+ * report. */
+int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned flags, unsigned batch,
+                                  char *buf, size_t size);
+
+/* ------------------------------------------------------ memory helpers */
+
+/* Device memory for callers that do not link the CUDA runtime themselves. */
+void *mufft_gb_device_alloc(size_t size);
+void mufft_gb_device_free(void *ptr);
+/* Synchronous copy between any two addresses the driver knows (host, pinned,
+ * device, managed). */
+int mufft_gb_memcpy(void *dst, const void *src, size_t size);
+int mufft_gb_device_synchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

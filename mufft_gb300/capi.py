@@ -1,0 +1,260 @@
+"""ctypes mirror of the muFFT C API (fft.h) and the GB300 extensions.
+
+`MuFFT(path, prefix)` binds any library that exports the fft.h functions
+under `prefix` ("mufft_" for libmufft_gb300.so and for the reference library;
+the oracle uses "oracle_").  Method names are the C names without the
+prefix, with the same arguments and the same NULL-on-error behaviour, so a
+test written against one library runs unchanged against the others.  The
+numpy helpers at the bottom (`fft_c2c`, `fft_r2c`, ...) wrap the
+create / execute / free sequence the reference's own tests use (test.c).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+FORWARD = -1
+INVERSE = 1
+FLAG_CPU_ANY = 0
+FLAG_CPU_NO_SIMD = (1 << 16) - 1
+FLAG_CPU_NO_AVX = 1 << 0
+FLAG_CPU_NO_SSE3 = 1 << 1
+FLAG_CPU_NO_SSE = 1 << 2
+FLAG_FULL_R2C = 1 << 16
+FLAG_ZERO_PAD_UPPER_HALF = 1 << 17
+CONV_METHOD_FLAG_MONO_MONO = 0
+CONV_METHOD_FLAG_STEREO_MONO = 1
+CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST = 1 << 2
+CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND = 1 << 3
+CONV_BLOCK_FIRST = 0
+CONV_BLOCK_SECOND = 1
+
+_vp = C.c_void_p
+_u = C.c_uint
+_i = C.c_int
+_sz = C.c_size_t
+
+# (name, restype, argtypes) of every fft.h entry point.
+FFT_H = [
+    ("create_plan_1d_c2c", _vp, [_u, _i, _u]),
+    ("create_plan_1d_r2c", _vp, [_u, _u]),
+    ("create_plan_1d_c2r", _vp, [_u, _u]),
+    ("execute_plan_1d", None, [_vp, _vp, _vp]),
+    ("free_plan_1d", None, [_vp]),
+    ("create_plan_conv", _vp, [_u, _u, _u]),
+    ("execute_conv_input", None, [_vp, _u, _vp, _vp]),
+    ("conv_get_transformed_block_size", _sz, [_vp]),
+    ("execute_conv_output", None, [_vp, _vp, _vp, _vp]),
+    ("free_plan_conv", None, [_vp]),
+    ("create_plan_2d_c2c", _vp, [_u, _u, _i, _u]),
+    ("create_plan_2d_r2c", _vp, [_u, _u, _u]),
+    ("create_plan_2d_c2r", _vp, [_u, _u, _u]),
+    ("execute_plan_2d", None, [_vp, _vp, _vp]),
+    ("free_plan_2d", None, [_vp]),
+]
+MEMORY_H = [
+    ("alloc", _vp, [_sz]),
+    ("calloc", _vp, [_sz]),
+    ("free", None, [_vp]),
+    ("get_convolve_func", _vp, [_u]),
+]
+# mufft_gb300.h (prefix mufft_gb_)
+GB_H = [
+    ("last_error", _i, []),
+    ("last_error_string", C.c_char_p, []),
+    ("clear_error", None, []),
+    ("create_plan_1d_c2c_batched", _vp, [_u, _i, _u, _u, _sz, _sz]),
+    ("create_plan_1d_r2c_batched", _vp, [_u, _u, _u, _sz, _sz]),
+    ("create_plan_1d_c2r_batched", _vp, [_u, _u, _u, _sz, _sz]),
+    ("execute_plan_1d_async", _i, [_vp, _vp, _vp, _vp]),
+    ("execute_plan_1d_launches_async", _i, [_vp, _vp, _vp, _u, _u, _vp]),
+    ("execute_plan_2d_async", _i, [_vp, _vp, _vp, _vp]),
+    ("execute_conv_input_async", _i, [_vp, _u, _vp, _vp, _vp]),
+    ("execute_conv_output_async", _i, [_vp, _vp, _vp, _vp, _vp]),
+    ("plan_1d_launches", _u, [_vp]),
+    ("plan_2d_launches", _u, [_vp]),
+    ("plan_1d_describe", _i, [_vp, C.c_char_p, _sz]),
+    ("plan_2d_describe", _i, [_vp, C.c_char_p, _sz]),
+    ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, C.c_char_p, _sz]),
+    ("device_alloc", _vp, [_sz]),
+    ("device_free", None, [_vp]),
+    ("memcpy", _i, [_vp, _vp, _sz]),
+    ("device_synchronize", _i, []),
+]
+
+CONVOLVE_FUNC = C.CFUNCTYPE(None, _vp, _vp, _vp, C.c_float, _u)
+
+
+class MuFFTError(RuntimeError):
+    pass
+
+
+def aligned_empty(shape, dtype, align: int = 64) -> np.ndarray:
+    """Uninitialised numpy array whose data starts on an `align`-byte boundary
+    (muFFT's contract for every buffer, fft_internal.h:38)."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) if np.ndim(shape) else int(shape)
+    raw = np.empty(n * dtype.itemsize + align, np.uint8)
+    off = (-raw.ctypes.data) % align
+    return raw[off: off + n * dtype.itemsize].view(dtype).reshape(shape)
+
+
+def aligned_zeros(shape, dtype) -> np.ndarray:
+    a = aligned_empty(shape, dtype)
+    a[...] = 0
+    return a
+
+
+def aligned_copy(x, dtype) -> np.ndarray:
+    x = np.asarray(x, dtype=dtype)
+    a = aligned_empty(x.shape, dtype)
+    a[...] = x
+    return a
+
+
+def _ptr(a) -> int:
+    """Address of a numpy array or torch tensor (or an int address)."""
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+class MuFFT:
+    """Binding of one library exporting the muFFT API under `prefix`."""
+
+    def __init__(self, path: str | Path, prefix: str = "mufft_", gb_extensions: bool = False):
+        self.path = str(path)
+        self.lib = C.CDLL(self.path)
+        self.prefix = prefix
+        self.symbols: list[str] = []
+        for name, res, args in FFT_H:
+            self._bind(prefix + name, name, res, args)
+        for name, res, args in MEMORY_H:
+            if hasattr(self.lib, prefix + name):
+                self._bind(prefix + name, name, res, args)
+        self.gb = gb_extensions
+        if gb_extensions:
+            for name, res, args in GB_H:
+                self._bind("mufft_gb_" + name, "gb_" + name, res, args)
+
+    def _bind(self, cname: str, pyname: str, res, args):
+        f = getattr(self.lib, cname)
+        f.restype = res
+        f.argtypes = args
+        setattr(self, pyname, f)
+        self.symbols.append(cname)
+
+    # ----------------------------------------------------------- errors
+    def check(self, what: str = "call"):
+        if self.gb:
+            code = self.gb_last_error()
+            if code:
+                msg = self.gb_last_error_string().decode()
+                self.gb_clear_error()
+                raise MuFFTError(f"{what}: error {code}: {msg}")
+
+    def _plan(self, p, what):
+        if not p:
+            if self.gb:
+                self.check(what)
+            raise MuFFTError(f"{what} returned NULL")
+        return p
+
+    # ---------------------------------------------------- numpy helpers
+    def fft_c2c(self, x: np.ndarray, direction: int, flags: int = 0, N: int | None = None) -> np.ndarray:
+        x = aligned_copy(x, np.complex64)
+        N = N or x.shape[-1]
+        plan = self._plan(self.create_plan_1d_c2c(N, direction, flags), "create_plan_1d_c2c")
+        out = aligned_zeros(N, np.complex64)
+        try:
+            self.execute_plan_1d(plan, _ptr(out), _ptr(x))
+            self.check("execute_plan_1d")
+        finally:
+            self.free_plan_1d(plan)
+        return out
+
+    def fft_r2c(self, x: np.ndarray, flags: int = 0, N: int | None = None) -> np.ndarray:
+        x = aligned_copy(x, np.float32)
+        N = N or x.shape[-1]
+        plan = self._plan(self.create_plan_1d_r2c(N, flags), "create_plan_1d_r2c")
+        nout = N if flags & FLAG_FULL_R2C else N // 2 + 1
+        out = aligned_zeros(nout, np.complex64)
+        try:
+            self.execute_plan_1d(plan, _ptr(out), _ptr(x))
+            self.check("execute_plan_1d")
+        finally:
+            self.free_plan_1d(plan)
+        return out
+
+    def fft_c2r(self, X: np.ndarray, N: int, flags: int = 0) -> np.ndarray:
+        X = aligned_copy(X, np.complex64)
+        assert X.shape[-1] >= N // 2 + 1
+        plan = self._plan(self.create_plan_1d_c2r(N, flags), "create_plan_1d_c2r")
+        out = aligned_zeros(N, np.float32)
+        try:
+            self.execute_plan_1d(plan, _ptr(out), _ptr(X))
+            self.check("execute_plan_1d")
+        finally:
+            self.free_plan_1d(plan)
+        return out
+
+    def conv(self, a: np.ndarray, b: np.ndarray, N: int, method: int, flags: int = 0) -> np.ndarray:
+        """Full muFFT convolution sequence: transform both blocks, multiply, inverse."""
+        stereo = (method & 1) == CONV_METHOD_FLAG_STEREO_MONO
+        a = aligned_copy(a, np.complex64 if stereo else np.float32)
+        b = aligned_copy(b, np.float32)
+        plan = self._plan(self.create_plan_conv(N, flags, method), "create_plan_conv")
+        try:
+            nblk = self.conv_get_transformed_block_size(plan) // 8
+            b0 = aligned_zeros(nblk, np.complex64)
+            b1 = aligned_zeros(nblk, np.complex64)
+            out = aligned_zeros(N, np.complex64 if stereo else np.float32)
+            self.execute_conv_input(plan, CONV_BLOCK_FIRST, _ptr(b0), _ptr(a))
+            self.execute_conv_input(plan, CONV_BLOCK_SECOND, _ptr(b1), _ptr(b))
+            self.execute_conv_output(plan, _ptr(out), _ptr(b0), _ptr(b1))
+            self.check("conv")
+        finally:
+            self.free_plan_conv(plan)
+        return out
+
+    def fft2_c2c(self, x: np.ndarray, direction: int, flags: int = 0) -> np.ndarray:
+        x = aligned_copy(x, np.complex64)
+        Ny, Nx = x.shape
+        plan = self._plan(self.create_plan_2d_c2c(Nx, Ny, direction, flags), "create_plan_2d_c2c")
+        out = aligned_zeros((Ny, Nx), np.complex64)
+        try:
+            self.execute_plan_2d(plan, _ptr(out), _ptr(x))
+            self.check("execute_plan_2d")
+        finally:
+            self.free_plan_2d(plan)
+        return out
+
+    def fft2_r2c(self, x: np.ndarray, flags: int = 0) -> np.ndarray:
+        """Returns the Ny x Nx complex output buffer (valid columns Nx/2 + 1, or Nx with FULL_R2C)."""
+        x = aligned_copy(x, np.float32)
+        Ny, Nx = x.shape
+        plan = self._plan(self.create_plan_2d_r2c(Nx, Ny, flags), "create_plan_2d_r2c")
+        out = aligned_zeros((Ny, Nx), np.complex64)
+        try:
+            self.execute_plan_2d(plan, _ptr(out), _ptr(x))
+            self.check("execute_plan_2d")
+        finally:
+            self.free_plan_2d(plan)
+        return out
+
+    def fft2_c2r(self, X: np.ndarray, flags: int = 0) -> np.ndarray:
+        """X: Ny x Nx complex buffer (first Nx/2 + 1 columns read); returns Ny x Nx reals."""
+        X = aligned_copy(X, np.complex64)
+        Ny, Nx = X.shape
+        plan = self._plan(self.create_plan_2d_c2r(Nx, Ny, flags), "create_plan_2d_c2r")
+        out = aligned_zeros(2 * Nx * Ny, np.float32)  # the reference's scratch contract (fft.h:258-260)
+        try:
+            self.execute_plan_2d(plan, _ptr(out), _ptr(X))
+            self.check("execute_plan_2d")
+        finally:
+            self.free_plan_2d(plan)
+        return out[: Nx * Ny].reshape(Ny, Nx)

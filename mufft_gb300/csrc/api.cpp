@@ -1,0 +1,1259 @@
+// Host side of libmufft_gb300: the muFFT C API (fft.h) and its GB300
+// extensions (mufft_gb300.h).
+//
+// Plan creation mirrors the reference constructors (fft.c:441-792): the same
+// argument checks and NULL returns, the same buffer-size contracts.  Where the
+// reference builds a list of CPU passes (fft.c:325-435), this file builds a
+// list of GPU launches:
+//   - complex length M <= 16384: one tile-FFT launch (one HBM read + write per
+//     transform), with the r2c/c2r fix-up and the convolution multiply fused
+//     into its load or store phase;
+//   - M > 16384: a four-step pair, M = N1 x N2: column FFTs of length N1 with
+//     the W_M^(k1*n2) twiddle fused into their stores, then row FFTs of length
+//     N2 with transposed stores into natural order.
+// Executes enqueue those launches on a stream.  The fft.h executes stage host
+// buffers through plan-owned device memory and synchronise before returning,
+// like the reference's synchronous calls (fft.c:811-989).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fft.h"
+#include "../../include/mufft_gb300.h"
+#include "common.h"
+#include "misc_kernels.h"
+#include "registry.h"
+
+using namespace mgb;
+
+// ================================================================ errors
+
+namespace {
+
+thread_local int t_err = 0;
+thread_local char t_errmsg[512] = "";
+
+void set_error(int code, const char *fmt, ...)
+{
+    t_err = code;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_errmsg, sizeof(t_errmsg), fmt, ap);
+    va_end(ap);
+}
+
+bool cuda_ok(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess)
+        return true;
+    set_error((int)e, "%s: %s", what, cudaGetErrorString(e));
+    return false;
+}
+
+bool is_pow2(unsigned n) { return n != 0 && (n & (n - 1)) == 0; }
+
+unsigned ilog2u(unsigned long long n)
+{
+    unsigned l = 0;
+    while ((1ull << l) < n)
+        l++;
+    return l;
+}
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        if (dev >= 0 && dev != prev)
+            cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+            cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+// ============================================================= registry
+
+namespace mgb {
+
+static std::vector<TileKernel> &tile_table()
+{
+    static std::vector<TileKernel> t = [] {
+        std::vector<TileKernel> v;
+        register_tiles_along(v);
+        register_tiles_across(v);
+        register_tiles_transpose(v);
+        return v;
+    }();
+    return t;
+}
+
+const TileKernel *find_tile(int L, int lmap, int smap)
+{
+    for (const TileKernel &k : tile_table())
+        if (k.L == L && k.lmap == lmap && k.smap == smap)
+            return &k;
+    return nullptr;
+}
+
+}  // namespace mgb
+
+// ======================================================== device state
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+struct DeviceState {
+    bool ready = false;
+    float2 *tw = nullptr;  // exp(-2*pi*i*j/kMaxTile)
+};
+
+std::mutex g_dev_mu;
+DeviceState g_dev[kMaxDevices];
+
+// Makes sure the current device has its twiddle table and kernel attributes.
+bool device_prepare(int *dev_out)
+{
+    int dev = -1;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        set_error(MUFFT_GB_ERR_NO_DEVICE, "no CUDA device visible");
+        return false;
+    }
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice"))
+        return false;
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "device index %d out of range", dev);
+        return false;
+    }
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    DeviceState &ds = g_dev[dev];
+    if (!ds.ready) {
+        std::vector<float2> h(kMaxTile);
+        for (unsigned j = 0; j < kMaxTile; j++) {
+            double ph = -2.0 * M_PI * (double)j / (double)kMaxTile;
+            h[j] = make_float2((float)std::cos(ph), (float)std::sin(ph));
+        }
+        if (!cuda_ok(cudaMalloc(&ds.tw, kMaxTile * sizeof(float2)), "cudaMalloc(twiddles)"))
+            return false;
+        if (!cuda_ok(cudaMemcpy(ds.tw, h.data(), kMaxTile * sizeof(float2), cudaMemcpyHostToDevice),
+                     "cudaMemcpy(twiddles)"))
+            return false;
+        for (const TileKernel &k : tile_table()) {
+            if (k.smem > 48 * 1024) {
+                if (!cuda_ok(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)k.smem),
+                             "cudaFuncSetAttribute"))
+                    return false;
+            }
+        }
+        ds.ready = true;
+    }
+    *dev_out = dev;
+    return true;
+}
+
+// Host-generated FP64 tables, rounded once to float.
+std::vector<float2> r2c_twiddles(int dir, unsigned M)
+{
+    // i*dir*exp(i*pi*dir*k/M) (fft.c:441-455)
+    std::vector<float2> t(M);
+    for (unsigned k = 0; k < M; k++) {
+        double ph = (M_PI * dir * (double)k) / (double)M;
+        double c = std::cos(ph), s = std::sin(ph);
+        t[k] = make_float2((float)(-dir * s), (float)(dir * c));
+    }
+    return t;
+}
+
+float2 *upload(const std::vector<float2> &h)
+{
+    float2 *d = nullptr;
+    if (!cuda_ok(cudaMalloc(&d, h.size() * sizeof(float2)), "cudaMalloc(table)"))
+        return nullptr;
+    if (!cuda_ok(cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(table)")) {
+        cudaFree(d);
+        return nullptr;
+    }
+    return d;
+}
+
+bool is_device_accessible(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// ================================================================ passes
+
+enum Role { ROLE_NONE = 0, ROLE_IN, ROLE_OUT, ROLE_IN2, ROLE_SCRATCH };
+enum PassType { PASS_TILE = 0, PASS_R2C_FIXUP = 1 };
+
+struct Pass {
+    PassType type = PASS_TILE;
+    const TileKernel *k = nullptr;
+    TileArgs a{};
+    Role in_role = ROLE_IN, out_role = ROLE_OUT, in2_role = ROLE_NONE;
+    dim3 grid;
+    // in-place r2c fix-up
+    long long M = 0, dist = 0;
+    unsigned batch = 1;
+    int full = 0;
+};
+
+struct Buffers {
+    const void *in;
+    void *out;
+    const void *in2;
+    void *scratch;
+};
+
+const void *pick(Role r, const Buffers &b)
+{
+    switch (r) {
+    case ROLE_IN: return b.in;
+    case ROLE_OUT: return b.out;
+    case ROLE_IN2: return b.in2;
+    case ROLE_SCRATCH: return b.scratch;
+    default: return nullptr;
+    }
+}
+
+cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream_t st, size_t first = 0,
+                       size_t count = (size_t)-1)
+{
+    for (size_t i = first; i < ps.size() && i - first < count; i++) {
+        const Pass &p = ps[i];
+        if (p.type == PASS_TILE) {
+            TileArgs a = p.a;
+            a.in = (const float2 *)pick(p.in_role, b);
+            a.out = (float2 *)pick(p.out_role, b);
+            a.in2 = (const float2 *)pick(p.in2_role, b);
+            void *args[] = {&a};
+            cudaError_t e = cudaLaunchKernel(p.k->fn, p.grid, dim3(p.k->threads), args, p.k->smem, st);
+            if (e != cudaSuccess)
+                return e;
+        } else {
+            cudaError_t e = launch_r2c_fixup_inplace((float2 *)pick(p.out_role, b), p.a.rtw, p.M, p.dist,
+                                                     p.batch, p.full, st);
+            if (e != cudaSuccess)
+                return e;
+        }
+    }
+    return cudaSuccess;
+}
+
+const char *pro_name(int p)
+{
+    static const char *n[] = {"plain", "c2r", "mul", "mul_c2r"};
+    return (p >= 0 && p < 4) ? n[p] : "?";
+}
+const char *epi_name(int e)
+{
+    static const char *n[] = {"plain", "r2c", "r2c_full", "twiddle"};
+    return (e >= 0 && e < 4) ? n[e] : "?";
+}
+
+std::string describe(const std::vector<Pass> &ps)
+{
+    std::string s;
+    char buf[256];
+    for (size_t i = 0; i < ps.size(); i++) {
+        const Pass &p = ps[i];
+        if (p.type == PASS_TILE)
+            snprintf(buf, sizeof(buf), "%stile L=%d R=%d C=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s conj=%d",
+                     i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->lmap ? "across" : "along",
+                     p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
+                     pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue), p.a.conj);
+        else
+            snprintf(buf, sizeof(buf), "%sr2c_fixup M=%lld batch=%u full=%d", i ? "; " : "", p.M, p.batch, p.full);
+        s += buf;
+    }
+    return s;
+}
+
+// One complex FFT stage group: `batch` transforms of length M.
+struct FftSpec {
+    unsigned M = 0;
+    unsigned batch = 1;
+    long long in_dist = 0, out_dist = 0;  // float2 units
+    int prologue = PRO_PLAIN;
+    int half = 0;
+    int epilogue = EPI_PLAIN;             // PLAIN, R2C or R2C_FULL
+    int conj_in = 0, conj_out = 0;
+    Role in_role = ROLE_IN, out_role = ROLE_OUT, in2_role = ROLE_NONE;
+    float scale = 1.0f;
+};
+
+// Device tables and scratch a schedule needs; allocated unless `dry`.
+struct PlanResources {
+    float2 *rtw = nullptr;
+    float2 *twA = nullptr, *twB = nullptr;
+    float2 *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void release()
+    {
+        cudaFree(rtw);
+        cudaFree(twA);
+        cudaFree(twB);
+        cudaFree(scratch);
+        rtw = twA = twB = scratch = nullptr;
+    }
+};
+
+bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bool dry,
+                      std::vector<Pass> &out)
+{
+    const unsigned M = s.M;
+    const bool r2c = s.epilogue == EPI_R2C || s.epilogue == EPI_R2C_FULL;
+    if (M <= kMaxTile) {
+        const TileKernel *k = find_tile((int)M, ALONG, ALONG);
+        if (!k) {
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "no tile kernel for length %u", M);
+            return false;
+        }
+        Pass p;
+        p.k = k;
+        p.a.in_stride = 1;
+        p.a.in_dist = s.in_dist;
+        p.a.out_stride = 1;
+        p.a.out_dist = s.out_dist;
+        p.a.ntrans = s.batch;
+        p.a.conj = (s.conj_in ? 1 : 0) | (s.conj_out ? 2 : 0);
+        p.a.prologue = s.prologue;
+        p.a.half = s.half;
+        p.a.epilogue = s.epilogue;
+        p.a.tw = tw;
+        p.a.rtw = res.rtw;
+        p.a.mirror_len = M;
+        p.a.mirror_ldist = 0;
+        p.a.scale = s.scale;
+        p.in_role = s.in_role;
+        p.out_role = s.out_role;
+        p.in2_role = s.in2_role;
+        p.grid = dim3((s.batch + k->C - 1) / k->C, 1);
+        out.push_back(p);
+        return true;
+    }
+
+    // Four-step: M = N1 * N2, x[n1*N2 + n2], X[k1 + N1*k2].
+    const unsigned lg = ilog2u(M);
+    const unsigned N1 = 1u << (lg / 2), N2 = M / N1;
+    if (N2 > kMaxTile) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "transform length %u exceeds the two-pass limit", M);
+        return false;
+    }
+    if (s.batch > 65535) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "batch %u too large for multi-pass lengths", s.batch);
+        return false;
+    }
+    const TileKernel *kc = find_tile((int)N1, ACROSS, ACROSS);
+    const TileKernel *kr = find_tile((int)N2, ALONG, ACROSS);
+    if (!kc || !kr) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "no four-step kernels for %u x %u", N1, N2);
+        return false;
+    }
+    const unsigned twbits = (lg + 1) / 2;
+    if (!dry) {
+        std::vector<float2> hb(1u << twbits), ha((M >> twbits) + 1);
+        for (size_t b = 0; b < hb.size(); b++) {
+            double ph = -2.0 * M_PI * (double)b / (double)M;
+            hb[b] = make_float2((float)std::cos(ph), (float)std::sin(ph));
+        }
+        for (size_t a = 0; a < ha.size(); a++) {
+            unsigned long long m = ((unsigned long long)a << twbits) % M;
+            double ph = -2.0 * M_PI * (double)m / (double)M;
+            ha[a] = make_float2((float)std::cos(ph), (float)std::sin(ph));
+        }
+        res.twA = upload(ha);
+        res.twB = upload(hb);
+        res.scratch_bytes = (size_t)M * s.batch * sizeof(float2);
+        if (!res.twA || !res.twB ||
+            !cuda_ok(cudaMalloc(&res.scratch, res.scratch_bytes), "cudaMalloc(scratch)"))
+            return false;
+    }
+    Pass p1;
+    p1.k = kc;
+    p1.a.in_stride = N2;
+    p1.a.in_dist = 1;
+    p1.a.in_batch = s.in_dist;
+    p1.a.out_stride = N2;
+    p1.a.out_dist = 1;
+    p1.a.out_batch = M;
+    p1.a.ntrans = N2;
+    p1.a.conj = s.conj_in ? 1 : 0;
+    p1.a.prologue = s.prologue;
+    p1.a.half = s.half;
+    p1.a.epilogue = EPI_TWIDDLE;
+    p1.a.tw = tw;
+    p1.a.rtw = res.rtw;
+    p1.a.mirror_len = M;
+    p1.a.mirror_ldist = 1;
+    p1.a.scale = s.scale;
+    p1.a.twA = res.twA;
+    p1.a.twB = res.twB;
+    p1.a.twbits = twbits;
+    p1.in_role = s.in_role;
+    p1.in2_role = s.in2_role;
+    p1.out_role = ROLE_SCRATCH;
+    p1.grid = dim3((N2 + kc->C - 1) / kc->C, s.batch);
+    out.push_back(p1);
+
+    Pass p2;
+    p2.k = kr;
+    p2.a.in_stride = 1;
+    p2.a.in_dist = N2;
+    p2.a.in_batch = M;
+    p2.a.out_stride = N1;
+    p2.a.out_dist = 1;
+    p2.a.out_batch = s.out_dist;
+    p2.a.ntrans = N1;
+    p2.a.conj = s.conj_out ? 2 : 0;
+    p2.a.prologue = PRO_PLAIN;
+    p2.a.epilogue = EPI_PLAIN;
+    p2.a.tw = tw;
+    p2.in_role = ROLE_SCRATCH;
+    p2.out_role = s.out_role;
+    p2.grid = dim3((N1 + kr->C - 1) / kr->C, s.batch);
+    out.push_back(p2);
+
+    if (r2c) {
+        Pass p3;
+        p3.type = PASS_R2C_FIXUP;
+        p3.a.rtw = res.rtw;
+        p3.out_role = s.out_role;
+        p3.M = M;
+        p3.dist = s.out_dist;
+        p3.batch = s.batch;
+        p3.full = s.epilogue == EPI_R2C_FULL;
+        out.push_back(p3);
+    }
+    return true;
+}
+
+// Lazily allocated device staging for host-memory arguments.
+struct Staging {
+    void *in = nullptr, *out = nullptr, *in2 = nullptr;
+    size_t in_bytes = 0, out_bytes = 0, in2_bytes = 0;
+    void release()
+    {
+        cudaFree(in);
+        cudaFree(out);
+        cudaFree(in2);
+        in = out = in2 = nullptr;
+        in_bytes = out_bytes = in2_bytes = 0;
+    }
+};
+
+bool ensure(void *&p, size_t &have, size_t need)
+{
+    if (have >= need && p)
+        return true;
+    cudaFree(p);
+    p = nullptr;
+    have = 0;
+    if (!cuda_ok(cudaMalloc(&p, need ? need : 16), "cudaMalloc(staging)"))
+        return false;
+    have = need;
+    return true;
+}
+
+}  // namespace
+
+// ================================================================== 1D
+
+enum Kind1D { K_C2C = 0, K_R2C = 1, K_C2R = 2 };
+
+struct mufft_plan_1d {
+    int device = -1;
+    int kind = K_C2C;
+    unsigned N = 0, M = 0;
+    int direction = MUFFT_FORWARD;
+    unsigned flags = 0;
+    unsigned batch = 1;
+    size_t in_elem = 8, out_elem = 8;    // bytes per input / output element
+    size_t in_count = 0, out_count = 0;  // elements read / written per transform
+    size_t idist = 0, odist = 0;         // elements between transforms
+    std::vector<Pass> passes;
+    PlanResources res;
+    Staging stage;
+    cudaStream_t stream = nullptr;
+    bool uses_in2 = false;
+
+    size_t in_total() const { return ((size_t)(batch - 1) * idist + in_count) * in_elem; }
+    size_t out_total() const { return ((size_t)(batch - 1) * odist + out_count) * out_elem; }
+};
+
+namespace {
+
+void destroy_1d(mufft_plan_1d *pl)
+{
+    if (!pl)
+        return;
+    if (pl->device >= 0) {
+        DeviceGuard g(pl->device);
+        pl->res.release();
+        pl->stage.release();
+        if (pl->stream)
+            cudaStreamDestroy(pl->stream);
+    }
+    delete pl;
+}
+
+// prologue_override: PRO_MUL / PRO_MUL_C2R for convolution output plans.
+mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, unsigned batch,
+                         size_t idist, size_t odist, int prologue_override, bool dry,
+                         std::string *desc)
+{
+    t_err = 0;
+    if (!is_pow2(N) || N == 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "N=%u is not a power of two >= 2", N);
+        return nullptr;
+    }
+    if (kind == K_C2C && direction != MUFFT_FORWARD && direction != MUFFT_INVERSE) {
+        set_error(MUFFT_GB_ERR_INVALID, "direction must be MUFFT_FORWARD or MUFFT_INVERSE");
+        return nullptr;
+    }
+    if (kind != K_C2C && N < 4) {
+        // the inner complex transform would have length 1 (fft.c:478-481 via :628-631)
+        set_error(MUFFT_GB_ERR_INVALID, "real transforms need N >= 4");
+        return nullptr;
+    }
+    if (batch == 0) {
+        set_error(MUFFT_GB_ERR_INVALID, "batch must be >= 1");
+        return nullptr;
+    }
+    const bool zp = (flags & MUFFT_FLAG_ZERO_PAD_UPPER_HALF) != 0;
+    const bool full = (flags & MUFFT_FLAG_FULL_R2C) != 0;
+
+    mufft_plan_1d *pl = new mufft_plan_1d();
+    pl->kind = kind;
+    pl->N = N;
+    pl->M = kind == K_C2C ? N : N / 2;
+    pl->direction = kind == K_C2C ? direction : (kind == K_R2C ? MUFFT_FORWARD : MUFFT_INVERSE);
+    pl->flags = flags;
+    pl->batch = batch;
+    const unsigned M = pl->M;
+
+    FftSpec s;
+    s.M = M;
+    s.batch = batch;
+    switch (kind) {
+    case K_C2C:
+        pl->in_elem = pl->out_elem = 8;
+        pl->in_count = zp ? N / 2 : N;
+        pl->out_count = N;
+        s.epilogue = EPI_PLAIN;
+        s.conj_in = s.conj_out = direction == MUFFT_INVERSE;
+        break;
+    case K_R2C:
+        pl->in_elem = 4;
+        pl->out_elem = 8;
+        pl->in_count = zp ? N / 2 : N;
+        pl->out_count = full ? N : N / 2 + 1;
+        s.epilogue = full ? EPI_R2C_FULL : EPI_R2C;
+        break;
+    case K_C2R:
+        pl->in_elem = 8;
+        pl->out_elem = 4;
+        pl->in_count = N / 2 + 1;
+        pl->out_count = N;
+        s.prologue = PRO_C2R;
+        s.conj_in = s.conj_out = 1;
+        break;
+    }
+    s.half = zp;
+    if (prologue_override >= 0) {
+        s.prologue = prologue_override;
+        s.in2_role = ROLE_IN2;
+        pl->uses_in2 = true;
+    }
+    // r2c input of N reals is read as M complex pairs.
+    pl->idist = idist ? idist : (kind == K_R2C ? (zp ? N / 2 : N) : pl->in_count);
+    pl->odist = odist ? odist : pl->out_count;
+    if ((kind == K_R2C && (pl->idist & 1)) || (kind == K_C2R && (pl->odist & 1))) {
+        set_error(MUFFT_GB_ERR_INVALID, "real-valued batch distances must be even");
+        delete pl;
+        return nullptr;
+    }
+    if (pl->idist < pl->in_count || pl->odist < pl->out_count) {
+        set_error(MUFFT_GB_ERR_INVALID, "batch distance smaller than one transform");
+        delete pl;
+        return nullptr;
+    }
+    s.in_dist = kind == K_R2C ? (long long)pl->idist / 2 : (long long)pl->idist;
+    s.out_dist = kind == K_C2R ? (long long)pl->odist / 2 : (long long)pl->odist;
+
+    const float2 *tw = nullptr;
+    if (!dry) {
+        int dev;
+        if (!device_prepare(&dev)) {
+            delete pl;
+            return nullptr;
+        }
+        pl->device = dev;
+        tw = g_dev[dev].tw;
+        if (kind != K_C2C) {
+            pl->res.rtw = upload(r2c_twiddles(kind == K_R2C ? MUFFT_FORWARD : MUFFT_INVERSE, M));
+            if (!pl->res.rtw) {
+                destroy_1d(pl);
+                return nullptr;
+            }
+        }
+        if (!cuda_ok(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
+            destroy_1d(pl);
+            return nullptr;
+        }
+    }
+    if (prologue_override >= 0 && kind == K_C2C)
+        s.scale = 1.0f / (float)N;
+    if (prologue_override >= 0 && kind == K_C2R)
+        s.scale = 1.0f / (float)N;
+    if (!build_fft_passes(s, tw, pl->res, dry, pl->passes)) {
+        destroy_1d(pl);
+        return nullptr;
+    }
+    if (desc)
+        *desc = describe(pl->passes);
+    if (dry) {
+        delete pl;
+        return nullptr;
+    }
+    return pl;
+}
+
+// Runs a 1D plan; `sync` selects the fft.h semantics (any memory, blocking).
+int exec_1d(mufft_plan_1d *pl, void *out, const void *in, const void *in2, cudaStream_t st, bool sync)
+{
+    if (!pl || !out || !in || (pl->uses_in2 && !in2)) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(pl->device);
+    const bool hin = !is_device_accessible(in);
+    const bool hin2 = pl->uses_in2 && !is_device_accessible(in2);
+    const bool hout = !is_device_accessible(out);
+    if (!sync && (hin || hin2 || hout)) {
+        set_error(MUFFT_GB_ERR_HOST_POINTER, "asynchronous execute needs device-accessible buffers");
+        return MUFFT_GB_ERR_HOST_POINTER;
+    }
+    if (sync)
+        st = pl->stream;
+    Buffers b{in, out, in2, pl->res.scratch};
+    if (hin) {
+        if (!ensure(pl->stage.in, pl->stage.in_bytes, pl->in_total()))
+            return t_err;
+        if (!cuda_ok(cudaMemcpyAsync(pl->stage.in, in, pl->in_total(), cudaMemcpyDefault, st), "H2D copy"))
+            return t_err;
+        b.in = pl->stage.in;
+    }
+    if (hin2) {
+        if (!ensure(pl->stage.in2, pl->stage.in2_bytes, pl->in_total()))
+            return t_err;
+        if (!cuda_ok(cudaMemcpyAsync(pl->stage.in2, in2, pl->in_total(), cudaMemcpyDefault, st), "H2D copy"))
+            return t_err;
+        b.in2 = pl->stage.in2;
+    }
+    if (hout) {
+        if (!ensure(pl->stage.out, pl->stage.out_bytes, pl->out_total()))
+            return t_err;
+        b.out = pl->stage.out;
+    }
+    if (!cuda_ok(run_passes(pl->passes, b, st), "kernel launch"))
+        return t_err;
+    if (hout && !cuda_ok(cudaMemcpyAsync(out, b.out, pl->out_total(), cudaMemcpyDefault, st), "D2H copy"))
+        return t_err;
+    if (sync && !cuda_ok(cudaStreamSynchronize(st), "execute"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mufft_plan_1d *mufft_create_plan_1d_c2c(unsigned N, int direction, unsigned flags)
+{
+    return create_1d(K_C2C, N, direction, flags, 1, 0, 0, -1, false, nullptr);
+}
+
+mufft_plan_1d *mufft_create_plan_1d_r2c(unsigned N, unsigned flags)
+{
+    return create_1d(K_R2C, N, MUFFT_FORWARD, flags, 1, 0, 0, -1, false, nullptr);
+}
+
+mufft_plan_1d *mufft_create_plan_1d_c2r(unsigned N, unsigned flags)
+{
+    return create_1d(K_C2R, N, MUFFT_INVERSE, flags, 1, 0, 0, -1, false, nullptr);
+}
+
+mufft_plan_1d *mufft_gb_create_plan_1d_c2c_batched(unsigned N, int direction, unsigned flags,
+                                                   unsigned batch, size_t idist, size_t odist)
+{
+    return create_1d(K_C2C, N, direction, flags, batch, idist, odist, -1, false, nullptr);
+}
+
+mufft_plan_1d *mufft_gb_create_plan_1d_r2c_batched(unsigned N, unsigned flags, unsigned batch,
+                                                   size_t idist, size_t odist)
+{
+    return create_1d(K_R2C, N, MUFFT_FORWARD, flags, batch, idist, odist, -1, false, nullptr);
+}
+
+mufft_plan_1d *mufft_gb_create_plan_1d_c2r_batched(unsigned N, unsigned flags, unsigned batch,
+                                                   size_t idist, size_t odist)
+{
+    return create_1d(K_C2R, N, MUFFT_INVERSE, flags, batch, idist, odist, -1, false, nullptr);
+}
+
+void mufft_execute_plan_1d(mufft_plan_1d *plan, void *MUFFT_RESTRICT output, const void *MUFFT_RESTRICT input)
+{
+    exec_1d(plan, output, input, nullptr, nullptr, true);
+}
+
+int mufft_gb_execute_plan_1d_launches_async(mufft_plan_1d *plan, void *output, const void *input,
+                                            unsigned first, unsigned count, void *stream)
+{
+    if (!plan || plan->uses_in2 || !is_device_accessible(output) || !is_device_accessible(input)) {
+        set_error(MUFFT_GB_ERR_INVALID, "needs a single-input plan and device buffers");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(plan->device);
+    Buffers b{input, output, nullptr, plan->res.scratch};
+    if (!cuda_ok(run_passes(plan->passes, b, (cudaStream_t)stream, first, count), "kernel launch"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_execute_plan_1d_async(mufft_plan_1d *plan, void *output, const void *input, void *stream)
+{
+    if (plan && plan->uses_in2) {
+        set_error(MUFFT_GB_ERR_INVALID, "plan needs two inputs");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    return exec_1d(plan, output, input, nullptr, (cudaStream_t)stream, false);
+}
+
+void mufft_free_plan_1d(mufft_plan_1d *plan) { destroy_1d(plan); }
+
+unsigned mufft_gb_plan_1d_launches(const mufft_plan_1d *plan) { return plan ? (unsigned)plan->passes.size() : 0; }
+
+int mufft_gb_plan_1d_describe(const mufft_plan_1d *plan, char *buf, size_t size)
+{
+    if (!plan || !buf || !size)
+        return MUFFT_GB_ERR_INVALID;
+    snprintf(buf, size, "%s", describe(plan->passes).c_str());
+    return MUFFT_GB_OK;
+}
+
+// Describes the launches a 1D plan would use, without a GPU.  kind: 0 c2c,
+// 1 r2c, 2 c2r.
+int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned flags, unsigned batch,
+                                  char *buf, size_t size)
+{
+    std::string d;
+    if (kind < 0 || kind > 2) {
+        set_error(MUFFT_GB_ERR_INVALID, "kind must be 0, 1 or 2");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    t_err = 0;
+    create_1d(kind, N, direction, flags, batch, 0, 0, -1, true, &d);
+    if (t_err)
+        return t_err;
+    if (buf && size)
+        snprintf(buf, size, "%s", d.c_str());
+    return MUFFT_GB_OK;
+}
+
+}  // extern "C"
+
+// ================================================================ conv
+
+struct mufft_plan_conv {
+    unsigned N = 0;
+    unsigned method = 0;
+    size_t block_size = 0;
+    mufft_plan_1d *in_plan[2] = {nullptr, nullptr};
+    mufft_plan_1d *out_plan = nullptr;
+};
+
+extern "C" {
+
+mufft_plan_conv *mufft_create_plan_conv(unsigned N, unsigned flags, unsigned method)
+{
+    t_err = 0;
+    if (!is_pow2(N) || N == 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "N=%u is not a power of two >= 2", N);
+        return nullptr;
+    }
+    mufft_plan_conv *c = new mufft_plan_conv();
+    c->N = N;
+    c->method = method;
+    const unsigned zp0 = (method & MUFFT_CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST) ? MUFFT_FLAG_ZERO_PAD_UPPER_HALF : 0;
+    const unsigned zp1 = (method & MUFFT_CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND) ? MUFFT_FLAG_ZERO_PAD_UPPER_HALF : 0;
+    const unsigned base = flags & ~(unsigned)MUFFT_FLAG_ZERO_PAD_UPPER_HALF;
+    if ((method & 1u) == MUFFT_CONV_METHOD_FLAG_STEREO_MONO) {
+        // fft.c:593-599
+        c->block_size = (size_t)N * 8;
+        c->in_plan[0] = create_1d(K_C2C, N, MUFFT_FORWARD, flags | zp0, 1, 0, 0, -1, false, nullptr);
+        c->in_plan[1] = create_1d(K_R2C, N, MUFFT_FORWARD, flags | zp1 | MUFFT_FLAG_FULL_R2C, 1, 0, 0, -1, false, nullptr);
+        c->out_plan = create_1d(K_C2C, N, MUFFT_INVERSE, base, 1, 0, 0, PRO_MUL, false, nullptr);
+    } else {
+        // fft.c:585-591
+        c->block_size = (size_t)(N / 2 + 4) * 8;
+        c->in_plan[0] = create_1d(K_R2C, N, MUFFT_FORWARD, flags | zp0, 1, 0, 0, -1, false, nullptr);
+        c->in_plan[1] = create_1d(K_R2C, N, MUFFT_FORWARD, flags | zp1, 1, 0, 0, -1, false, nullptr);
+        c->out_plan = create_1d(K_C2R, N, MUFFT_INVERSE, base, 1, 0, 0, PRO_MUL_C2R, false, nullptr);
+    }
+    if (!c->in_plan[0] || !c->in_plan[1] || !c->out_plan) {
+        mufft_free_plan_conv(c);
+        return nullptr;
+    }
+    return c;
+}
+
+void mufft_execute_conv_input(mufft_plan_conv *plan, unsigned block, void *output, const void *input)
+{
+    if (!plan) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan");
+        return;
+    }
+    exec_1d(plan->in_plan[block ? 1 : 0], output, input, nullptr, nullptr, true);
+}
+
+size_t mufft_conv_get_transformed_block_size(mufft_plan_conv *plan) { return plan ? plan->block_size : 0; }
+
+void mufft_execute_conv_output(mufft_plan_conv *plan, void *output, const void *input_first,
+                               const void *input_second)
+{
+    if (!plan) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan");
+        return;
+    }
+    exec_1d(plan->out_plan, output, input_first, input_second, nullptr, true);
+}
+
+int mufft_gb_execute_conv_input_async(mufft_plan_conv *plan, unsigned block, void *output,
+                                      const void *input, void *stream)
+{
+    if (!plan) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    return exec_1d(plan->in_plan[block ? 1 : 0], output, input, nullptr, (cudaStream_t)stream, false);
+}
+
+int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, const void *input_first,
+                                       const void *input_second, void *stream)
+{
+    if (!plan) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    return exec_1d(plan->out_plan, output, input_first, input_second, (cudaStream_t)stream, false);
+}
+
+void mufft_free_plan_conv(mufft_plan_conv *plan)
+{
+    if (!plan)
+        return;
+    destroy_1d(plan->in_plan[0]);
+    destroy_1d(plan->in_plan[1]);
+    destroy_1d(plan->out_plan);
+    delete plan;
+}
+
+}  // extern "C"
+
+// ======================================================= convolve func
+
+namespace {
+
+// Element-wise multiply for mufft_get_convolve_func: any memory, blocking.
+void gpu_convolve(void *output, const void *a, const void *b, float normalization, unsigned samples)
+{
+    if (!output || !a || !b) {
+        set_error(MUFFT_GB_ERR_INVALID, "null buffer");
+        return;
+    }
+    int dev;
+    if (!device_prepare(&dev))
+        return;
+    const size_t bytes = (size_t)samples * sizeof(float2);
+    const bool ha = !is_device_accessible(a), hb = !is_device_accessible(b), ho = !is_device_accessible(output);
+    float2 *da = (float2 *)a, *db = (float2 *)b, *dout = (float2 *)output;
+    float2 *tmp = nullptr;
+    if (ha || hb || ho) {
+        if (!cuda_ok(cudaMalloc(&tmp, 3 * bytes + 16), "cudaMalloc(convolve)"))
+            return;
+        if (ha) {
+            da = tmp;
+            cudaMemcpy(da, a, bytes, cudaMemcpyDefault);
+        }
+        if (hb) {
+            db = tmp + samples;
+            cudaMemcpy(db, b, bytes, cudaMemcpyDefault);
+        }
+        if (ho)
+            dout = tmp + 2 * (size_t)samples;
+    }
+    if (cuda_ok(launch_spectral_multiply(dout, da, db, normalization, samples, nullptr), "convolve")) {
+        if (ho)
+            cuda_ok(cudaMemcpy(output, dout, bytes, cudaMemcpyDefault), "D2H copy");
+        else
+            cuda_ok(cudaDeviceSynchronize(), "convolve");
+    }
+    cudaFree(tmp);
+}
+
+}  // namespace
+
+extern "C" mufft_convolve_func mufft_get_convolve_func(unsigned flags)
+{
+    (void)flags;
+    return &gpu_convolve;
+}
+
+// ================================================================== 2D
+
+enum Kind2D { K2_C2C = 0, K2_R2C = 1, K2_C2R = 2 };
+
+struct mufft_plan_2d {
+    int device = -1;
+    int kind = K2_C2C;
+    unsigned Nx = 0, Ny = 0, Mx = 0;
+    int direction = MUFFT_FORWARD;
+    unsigned flags = 0;
+    unsigned vertical_nx = 0;
+    std::vector<Pass> passes;
+    PlanResources res;
+    Staging stage;
+    cudaStream_t stream = nullptr;
+    // bytes moved for host buffers: rows x width inside rows of pitch
+    size_t in_rows = 0, in_width = 0, in_pitch = 0;
+    size_t out_rows = 0, out_width = 0, out_pitch = 0;
+};
+
+namespace {
+
+void destroy_2d(mufft_plan_2d *pl)
+{
+    if (!pl)
+        return;
+    if (pl->device >= 0) {
+        DeviceGuard g(pl->device);
+        pl->res.release();
+        pl->stage.release();
+        if (pl->stream)
+            cudaStreamDestroy(pl->stream);
+    }
+    delete pl;
+}
+
+mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsigned flags)
+{
+    t_err = 0;
+    if (!is_pow2(Nx) || !is_pow2(Ny) || Nx == 1 || Ny == 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "Nx=%u, Ny=%u must be powers of two >= 2", Nx, Ny);
+        return nullptr;
+    }
+    if (kind == K2_C2C && direction != MUFFT_FORWARD && direction != MUFFT_INVERSE) {
+        set_error(MUFFT_GB_ERR_INVALID, "direction must be MUFFT_FORWARD or MUFFT_INVERSE");
+        return nullptr;
+    }
+    if (kind != K2_C2C && Nx < 4) {
+        set_error(MUFFT_GB_ERR_INVALID, "real 2D transforms need Nx >= 4");
+        return nullptr;
+    }
+    const unsigned Mx = kind == K2_C2C ? Nx : Nx / 2;
+    if (Mx > kMaxTile || Ny > kMaxTile) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "2D side longer than %u", kMaxTile);
+        return nullptr;
+    }
+    const TileKernel *krow = find_tile((int)Mx, ALONG, ALONG);
+    const TileKernel *kcol = find_tile((int)Ny, ACROSS, ACROSS);
+    if (!krow || !kcol) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "no 2D kernels for %u x %u", Nx, Ny);
+        return nullptr;
+    }
+    int dev;
+    if (!device_prepare(&dev))
+        return nullptr;
+    mufft_plan_2d *pl = new mufft_plan_2d();
+    pl->device = dev;
+    pl->kind = kind;
+    pl->Nx = Nx;
+    pl->Ny = Ny;
+    pl->Mx = Mx;
+    pl->flags = flags;
+    pl->direction = kind == K2_C2C ? direction : (kind == K2_R2C ? MUFFT_FORWARD : MUFFT_INVERSE);
+    const float2 *tw = g_dev[dev].tw;
+    const bool inv = pl->direction == MUFFT_INVERSE;
+    const bool full = (flags & MUFFT_FLAG_FULL_R2C) != 0;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
+        destroy_2d(pl);
+        return nullptr;
+    }
+    if (kind != K2_C2C) {
+        pl->res.rtw = upload(r2c_twiddles(kind == K2_R2C ? MUFFT_FORWARD : MUFFT_INVERSE, Mx));
+        if (!pl->res.rtw) {
+            destroy_2d(pl);
+            return nullptr;
+        }
+    }
+
+    Pass row;
+    row.k = krow;
+    row.a.in_stride = 1;
+    row.a.out_stride = 1;
+    row.a.ntrans = Ny;
+    row.a.tw = tw;
+    row.a.rtw = pl->res.rtw;
+    row.a.mirror_len = Mx;
+    row.a.scale = 1.0f;
+    row.grid = dim3((Ny + krow->C - 1) / krow->C, 1);
+
+    Pass col;
+    col.k = kcol;
+    col.a.in_dist = 1;
+    col.a.out_dist = 1;
+    col.a.tw = tw;
+    col.a.scale = 1.0f;
+
+    if (kind == K2_C2C) {
+        // rows then columns in place (fft.c:917-988)
+        row.a.in_dist = Nx;
+        row.a.out_dist = Nx;
+        row.a.conj = inv ? 1 : 0;
+        col.a.in_stride = col.a.out_stride = Nx;
+        col.a.ntrans = Nx;
+        col.a.conj = inv ? 2 : 0;
+        col.in_role = ROLE_OUT;
+        col.out_role = ROLE_OUT;
+        pl->vertical_nx = Nx;
+        pl->in_rows = pl->out_rows = Ny;
+        pl->in_width = pl->out_width = pl->in_pitch = pl->out_pitch = (size_t)Nx * 8;
+    } else if (kind == K2_R2C) {
+        // rows with fused fix-up into a row stride of Nx complex, then the
+        // Nx/2 + 1 (or Nx) columns in place (fft.c:939-987, :738-746)
+        pl->vertical_nx = full ? Nx : Mx + 1;
+        row.a.in_dist = Mx;
+        row.a.out_dist = Nx;
+        row.a.epilogue = full ? EPI_R2C_FULL : EPI_R2C;
+        col.a.in_stride = col.a.out_stride = Nx;
+        col.a.ntrans = pl->vertical_nx;
+        col.in_role = ROLE_OUT;
+        col.out_role = ROLE_OUT;
+        pl->in_rows = Ny;
+        pl->in_width = pl->in_pitch = (size_t)Nx * 4;
+        pl->out_rows = Ny;
+        pl->out_width = (size_t)pl->vertical_nx * 8;
+        pl->out_pitch = (size_t)Nx * 8;
+    } else {
+        // columns first into scratch (Nx/2 + 1 of them), then rows with the
+        // fused c2r fix-up (fft.c:863-916)
+        pl->vertical_nx = Mx + 1;
+        const size_t sstride = Mx + 1;
+        pl->res.scratch_bytes = sstride * Ny * sizeof(float2);
+        if (!cuda_ok(cudaMalloc(&pl->res.scratch, pl->res.scratch_bytes), "cudaMalloc(scratch)")) {
+            destroy_2d(pl);
+            return nullptr;
+        }
+        col.a.in_stride = Nx;
+        col.a.out_stride = (long long)sstride;
+        col.a.ntrans = Mx + 1;
+        col.a.conj = 3;
+        col.in_role = ROLE_IN;
+        col.out_role = ROLE_SCRATCH;
+        row.a.in_dist = (long long)sstride;
+        row.a.out_dist = Mx;
+        row.a.prologue = PRO_C2R;
+        row.a.conj = 3;
+        row.in_role = ROLE_SCRATCH;
+        row.out_role = ROLE_OUT;
+        pl->in_rows = Ny;
+        pl->in_width = (size_t)(Mx + 1) * 8;
+        pl->in_pitch = (size_t)Nx * 8;
+        pl->out_rows = Ny;
+        pl->out_width = pl->out_pitch = (size_t)Nx * 4;
+    }
+    col.grid = dim3((col.a.ntrans + kcol->C - 1) / kcol->C, 1);
+    if (kind == K2_C2R) {
+        pl->passes.push_back(col);
+        pl->passes.push_back(row);
+    } else {
+        pl->passes.push_back(row);
+        pl->passes.push_back(col);
+    }
+    return pl;
+}
+
+int exec_2d(mufft_plan_2d *pl, void *out, const void *in, cudaStream_t st, bool sync)
+{
+    if (!pl || !out || !in) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(pl->device);
+    const bool hin = !is_device_accessible(in);
+    const bool hout = !is_device_accessible(out);
+    if (!sync && (hin || hout)) {
+        set_error(MUFFT_GB_ERR_HOST_POINTER, "asynchronous execute needs device-accessible buffers");
+        return MUFFT_GB_ERR_HOST_POINTER;
+    }
+    if (sync)
+        st = pl->stream;
+    Buffers b{in, out, nullptr, pl->res.scratch};
+    const size_t in_bytes = pl->in_rows * pl->in_pitch;
+    const size_t out_bytes = pl->out_rows * pl->out_pitch;
+    if (hin) {
+        if (!ensure(pl->stage.in, pl->stage.in_bytes, in_bytes))
+            return t_err;
+        if (!cuda_ok(cudaMemcpy2DAsync(pl->stage.in, pl->in_pitch, in, pl->in_pitch, pl->in_width,
+                                       pl->in_rows, cudaMemcpyDefault, st),
+                     "H2D copy"))
+            return t_err;
+        b.in = pl->stage.in;
+    }
+    if (hout) {
+        if (!ensure(pl->stage.out, pl->stage.out_bytes, out_bytes))
+            return t_err;
+        b.out = pl->stage.out;
+    }
+    if (!cuda_ok(run_passes(pl->passes, b, st), "kernel launch"))
+        return t_err;
+    if (hout && !cuda_ok(cudaMemcpy2DAsync(out, pl->out_pitch, b.out, pl->out_pitch, pl->out_width,
+                                           pl->out_rows, cudaMemcpyDefault, st),
+                         "D2H copy"))
+        return t_err;
+    if (sync && !cuda_ok(cudaStreamSynchronize(st), "execute"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mufft_plan_2d *mufft_create_plan_2d_c2c(unsigned Nx, unsigned Ny, int direction, unsigned flags)
+{
+    return create_2d(K2_C2C, Nx, Ny, direction, flags);
+}
+
+mufft_plan_2d *mufft_create_plan_2d_r2c(unsigned Nx, unsigned Ny, unsigned flags)
+{
+    return create_2d(K2_R2C, Nx, Ny, MUFFT_FORWARD, flags);
+}
+
+mufft_plan_2d *mufft_create_plan_2d_c2r(unsigned Nx, unsigned Ny, unsigned flags)
+{
+    return create_2d(K2_C2R, Nx, Ny, MUFFT_INVERSE, flags);
+}
+
+void mufft_execute_plan_2d(mufft_plan_2d *plan, void *MUFFT_RESTRICT output, const void *MUFFT_RESTRICT input)
+{
+    exec_2d(plan, output, input, nullptr, true);
+}
+
+int mufft_gb_execute_plan_2d_async(mufft_plan_2d *plan, void *output, const void *input, void *stream)
+{
+    return exec_2d(plan, output, input, (cudaStream_t)stream, false);
+}
+
+void mufft_free_plan_2d(mufft_plan_2d *plan) { destroy_2d(plan); }
+
+unsigned mufft_gb_plan_2d_launches(const mufft_plan_2d *plan) { return plan ? (unsigned)plan->passes.size() : 0; }
+
+int mufft_gb_plan_2d_describe(const mufft_plan_2d *plan, char *buf, size_t size)
+{
+    if (!plan || !buf || !size)
+        return MUFFT_GB_ERR_INVALID;
+    snprintf(buf, size, "%s", describe(plan->passes).c_str());
+    return MUFFT_GB_OK;
+}
+
+// ================================================================ memory
+
+void *mufft_alloc(size_t size)
+{
+    void *p = nullptr;
+    if (!cuda_ok(cudaMallocHost(&p, size ? size : 1), "cudaMallocHost"))
+        return nullptr;
+    return p;
+}
+
+void *mufft_calloc(size_t size)
+{
+    void *p = mufft_alloc(size);
+    if (p)
+        memset(p, 0, size);
+    return p;
+}
+
+void mufft_free(void *ptr)
+{
+    if (ptr)
+        cudaFreeHost(ptr);
+}
+
+void *mufft_gb_device_alloc(size_t size)
+{
+    void *p = nullptr;
+    if (!cuda_ok(cudaMalloc(&p, size ? size : 1), "cudaMalloc"))
+        return nullptr;
+    return p;
+}
+
+void mufft_gb_device_free(void *ptr)
+{
+    if (ptr)
+        cudaFree(ptr);
+}
+
+int mufft_gb_memcpy(void *dst, const void *src, size_t size)
+{
+    if (!cuda_ok(cudaMemcpy(dst, src, size, cudaMemcpyDefault), "cudaMemcpy"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_device_synchronize(void)
+{
+    if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+// ================================================================ errors
+
+int mufft_gb_last_error(void) { return t_err; }
+const char *mufft_gb_last_error_string(void) { return t_err ? t_errmsg : ""; }
+void mufft_gb_clear_error(void)
+{
+    t_err = 0;
+    t_errmsg[0] = 0;
+}
+
+}  // extern "C"

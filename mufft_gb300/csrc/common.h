@@ -1,0 +1,63 @@
+// Shared host/device definitions for the GB300 muFFT kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mgb {
+
+// Largest FFT length one CTA keeps on chip (registers + shared memory).
+constexpr unsigned kMaxTileLog2 = 14;
+constexpr unsigned kMaxTile = 1u << kMaxTileLog2;
+
+// Thread-to-work decomposition of a CTA: which index runs fastest across
+// consecutive threads.  ALONG: consecutive threads walk along one transform
+// (contiguous rows); ACROSS: consecutive threads walk across neighbouring
+// transforms (columns of a row-major grid, transposed stores).
+enum Map : int { ALONG = 0, ACROSS = 1 };
+
+// How stage-0 inputs are produced from global memory.
+enum Prologue : int {
+    PRO_PLAIN = 0,      // x[n]
+    PRO_C2R = 1,        // complex-to-real fix-up: (a + b*) + w_n (a - b*), a = X[n], b = X[M - n]
+    PRO_MUL = 2,        // s * A[n] * B[n]            (stereo convolution output)
+    PRO_MUL_C2R = 3,    // fix-up of s * A[n] * B[n]  (mono convolution output)
+};
+
+// How last-stage outputs are written.
+enum Epilogue : int {
+    EPI_PLAIN = 0,
+    EPI_R2C = 1,        // real-to-complex fix-up, M + 1 bins
+    EPI_R2C_FULL = 2,   // real-to-complex fix-up, all 2M bins
+    EPI_TWIDDLE = 3,    // four-step inter-pass twiddle W_N^(k * column)
+};
+
+// Arguments of one tile-FFT launch.  A launch runs `ntrans` transforms of
+// length L (times gridDim.y batches).  Element n of transform t lives at
+//     base + t * dist + n * stride
+// with base advanced by blockIdx.y * batch for batched multi-pass launches.
+struct TileArgs {
+    const float2 *in;
+    float2 *out;
+    long long in_stride, in_dist, in_batch;
+    long long out_stride, out_dist, out_batch;
+    unsigned ntrans;
+    int conj;                 // 1: inverse transform by conjugating in and out
+    int prologue;
+    int half;                 // inputs n >= L/2 are zero and not read (MUFFT_FLAG_ZERO_PAD_UPPER_HALF)
+    int epilogue;
+    const float2 *tw;         // exp(-2*pi*i*j/kMaxTile), j < kMaxTile
+    // real<->complex fix-ups: twiddles of length M, mirror length M
+    const float2 *rtw;
+    long long mirror_len;     // M for PRO_C2R / PRO_MUL_C2R
+    long long mirror_ldist;   // see tile kernel: local index = t*ldist + n*stride
+    // convolution prologues
+    const float2 *in2;        // second spectrum (B)
+    float scale;
+    // four-step twiddles: W_N^m = twA[m >> twbits] * twB[m & (2^twbits - 1)]
+    const float2 *twA;
+    const float2 *twB;
+    unsigned twbits;
+};
+
+}  // namespace mgb

@@ -1,0 +1,14 @@
+// Launchers of the element-wise kernels in misc_kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mgb {
+
+cudaError_t launch_r2c_fixup_inplace(float2 *z, const float2 *rtw, long long M, long long dist,
+                                     unsigned batch, int full, cudaStream_t st);
+cudaError_t launch_spectral_multiply(float2 *out, const float2 *a, const float2 *b, float s,
+                                     unsigned long long n, cudaStream_t st);
+cudaError_t launch_fill_u32(unsigned *p, unsigned v, unsigned long long n, cudaStream_t st);
+
+}  // namespace mgb

@@ -1,0 +1,27 @@
+// Table of compiled tile-FFT instantiations, filled by the kernel translation
+// units and searched by the planner.
+#pragma once
+
+#include <stddef.h>
+#include <vector>
+
+namespace mgb {
+
+struct TileKernel {
+    int L;          // transform length
+    int R;          // elements per thread
+    int C;          // transforms per CTA
+    int lmap, smap; // thread maps of the load and store phases
+    const void *fn;
+    int threads;
+    size_t smem;
+};
+
+void register_tiles_along(std::vector<TileKernel> &out);
+void register_tiles_across(std::vector<TileKernel> &out);
+void register_tiles_transpose(std::vector<TileKernel> &out);
+
+// Returns the instantiation for (L, lmap, smap), or nullptr.
+const TileKernel *find_tile(int L, int lmap, int smap);
+
+}  // namespace mgb

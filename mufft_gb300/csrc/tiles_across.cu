@@ -1,0 +1,30 @@
+// Column passes: loads and stores walk across neighbouring transforms, so a
+// warp touches C consecutive columns of each row it reads or writes.
+#include "fft_device.cuh"
+#include "registry.h"
+
+namespace mgb {
+
+#define TILE(L, R, C)                                                                              \
+    out.push_back(TileKernel{L, R, C, ACROSS, ACROSS, (const void *)&tile_fft<L, R, C, ACROSS, ACROSS>, \
+                             C *(L / R), tile_smem_bytes<L, R, C, ACROSS, ACROSS>()})
+
+void register_tiles_across(std::vector<TileKernel> &out)
+{
+    TILE(2, 2, 256);
+    TILE(4, 4, 256);
+    TILE(8, 8, 256);
+    TILE(16, 16, 256);
+    TILE(32, 16, 128);
+    TILE(64, 16, 64);
+    TILE(128, 16, 32);
+    TILE(256, 16, 16);
+    TILE(512, 16, 8);
+    TILE(1024, 16, 8);
+    TILE(2048, 16, 4);
+    TILE(4096, 32, 4);
+    TILE(8192, 32, 2);
+    TILE(16384, 32, 1);
+}
+
+}  // namespace mgb

@@ -1,0 +1,29 @@
+// Contiguous batched transforms: loads and stores walk along each transform.
+#include "fft_device.cuh"
+#include "registry.h"
+
+namespace mgb {
+
+#define TILE(L, R, C)                                                                          \
+    out.push_back(TileKernel{L, R, C, ALONG, ALONG, (const void *)&tile_fft<L, R, C, ALONG, ALONG>, \
+                             C *(L / R), tile_smem_bytes<L, R, C, ALONG, ALONG>()})
+
+void register_tiles_along(std::vector<TileKernel> &out)
+{
+    TILE(2, 2, 256);
+    TILE(4, 4, 256);
+    TILE(8, 8, 256);
+    TILE(16, 16, 256);
+    TILE(32, 16, 128);
+    TILE(64, 16, 64);
+    TILE(128, 16, 32);
+    TILE(256, 16, 16);
+    TILE(512, 16, 8);
+    TILE(1024, 16, 4);
+    TILE(2048, 16, 2);
+    TILE(4096, 16, 1);
+    TILE(8192, 32, 1);
+    TILE(16384, 32, 1);
+}
+
+}  // namespace mgb

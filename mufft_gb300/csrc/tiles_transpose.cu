@@ -1,0 +1,26 @@
+// Row passes with transposed stores (second pass of the four-step FFT): loads
+// walk along each row, stores walk across neighbouring rows.
+#include "fft_device.cuh"
+#include "registry.h"
+
+namespace mgb {
+
+#define TILE(L, R, C)                                                                              \
+    out.push_back(TileKernel{L, R, C, ALONG, ACROSS, (const void *)&tile_fft<L, R, C, ALONG, ACROSS>, \
+                             C *(L / R), tile_smem_bytes<L, R, C, ALONG, ACROSS>()})
+
+void register_tiles_transpose(std::vector<TileKernel> &out)
+{
+    TILE(32, 16, 128);
+    TILE(64, 16, 64);
+    TILE(128, 16, 32);
+    TILE(256, 16, 16);
+    TILE(512, 16, 8);
+    TILE(1024, 16, 8);
+    TILE(2048, 16, 4);
+    TILE(4096, 32, 4);
+    TILE(8192, 32, 2);
+    TILE(16384, 32, 1);
+}
+
+}  // namespace mgb

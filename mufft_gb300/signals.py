@@ -1,0 +1,50 @@
+"""Deterministic synthetic inputs shared by the tests, the bench and smoke().
+
+SplitMix64 streams (the same integers on every machine and numpy version),
+turned into float32 uniforms on [-1, 1) from the top 24 bits, and into
+normals by Box-Muller in float64.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        i = np.arange(offset + 1, offset + n + 1, dtype=np.uint64)
+        z = np.uint64(seed) * _M2 + i * _GAMMA
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """float32 uniform on [-1, 1): multiples of 2^-23."""
+    top = (splitmix64(seed, n, offset) >> np.uint64(40)).astype(np.int64)
+    return ((top - (1 << 23)).astype(np.float64) / float(1 << 23)).astype(np.float32)
+
+
+def normal(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """float32 standard normals (Box-Muller on two uniform streams)."""
+    u = (splitmix64(seed, 2 * n, 2 * offset) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    u1 = np.maximum(u[0::2], 1e-300)
+    u2 = u[1::2]
+    return (np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)).astype(np.float32)
+
+
+def complex_uniform(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """complex64 with re, im i.i.d. uniform on [-1, 1)."""
+    u = uniform(seed, 2 * n, 2 * offset)
+    return u.view(np.complex64)
+
+
+def complex_logmag(seed: int, n: int, lo: float = 1e-3, hi: float = 1e3) -> np.ndarray:
+    """complex64 with log-uniform magnitude on [lo, hi) and uniform phase."""
+    u = (splitmix64(seed, 2 * n) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    mag = np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * u[0::2])
+    ph = 2.0 * np.pi * u[1::2]
+    return (mag * np.exp(1j * ph)).astype(np.complex64)

@@ -1,0 +1,136 @@
+"""C-ABI checks that need no GPU: the library loads, exports exactly what
+include/*.h declares, validates arguments like the reference, and plans the
+GPU schedule on the host."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+import mufft_gb300
+from mufft_gb300 import capi as K
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _has_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def declared_functions() -> set[str]:
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(mufft_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return mufft_gb300.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = declared_functions()
+    assert len(declared) >= 38
+    for name in sorted(declared):
+        assert hasattr(lib.lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_reference_api_complete(lib):
+    # Every function of the reference fft.h (fft.h:86-297) is present.
+    ref_api = {"mufft_create_plan_1d_c2c", "mufft_create_plan_1d_r2c", "mufft_create_plan_1d_c2r",
+               "mufft_execute_plan_1d", "mufft_free_plan_1d", "mufft_create_plan_conv",
+               "mufft_execute_conv_input", "mufft_conv_get_transformed_block_size",
+               "mufft_execute_conv_output", "mufft_free_plan_conv", "mufft_get_convolve_func",
+               "mufft_create_plan_2d_c2c", "mufft_create_plan_2d_r2c", "mufft_create_plan_2d_c2r",
+               "mufft_execute_plan_2d", "mufft_free_plan_2d", "mufft_alloc", "mufft_calloc", "mufft_free"}
+    assert ref_api <= declared_functions()
+    for name in ref_api:
+        assert hasattr(lib.lib, name)
+
+
+def test_constants_match_reference():
+    h = (ROOT / "include" / "fft.h").read_text()
+    want = {"MUFFT_FORWARD": "(-1)", "MUFFT_INVERSE": "(1)", "MUFFT_FLAG_CPU_ANY": "(0)",
+            "MUFFT_FLAG_CPU_NO_SIMD": "((1 << 16) - 1)", "MUFFT_FLAG_FULL_R2C": "(1 << 16)",
+            "MUFFT_FLAG_ZERO_PAD_UPPER_HALF": "(1 << 17)",
+            "MUFFT_CONV_METHOD_FLAG_STEREO_MONO": "1",
+            "MUFFT_CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST": "(1 << 2)",
+            "MUFFT_CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND": "(1 << 3)",
+            "MUFFT_CONV_BLOCK_SECOND": "1"}
+    for k, v in want.items():
+        m = re.search(rf"#define {k}\s+(.+)", h)
+        assert m and m.group(1).strip() == v, k
+
+
+def test_null_frees_are_noops(lib):
+    lib.free_plan_1d(None)
+    lib.free_plan_2d(None)
+    lib.free_plan_conv(None)
+    lib.free(None)
+
+
+@pytest.mark.parametrize("N", [0, 1, 3, 12, 1000])
+def test_invalid_sizes_rejected(lib, N):
+    assert not lib.create_plan_1d_c2c(N, K.FORWARD, 0)
+    assert lib.gb_last_error() == -1  # MUFFT_GB_ERR_INVALID, decided before any device use
+    lib.gb_clear_error()
+    assert not lib.create_plan_1d_r2c(N, 0)
+    assert not lib.create_plan_conv(N, 0, 0)
+    assert not lib.create_plan_2d_c2c(N, 4, K.FORWARD, 0)
+    lib.gb_clear_error()
+
+
+def test_reference_edge_rejections(lib):
+    # r2c/c2r need N >= 4 (the inner complex transform of N/2 = 1 fails).
+    for f in (lib.create_plan_1d_r2c, lib.create_plan_1d_c2r):
+        assert not f(2, 0)
+        assert lib.gb_last_error() == -1
+        lib.gb_clear_error()
+    assert not lib.create_plan_1d_c2c(64, 0, 0)  # direction must be +-1
+    assert lib.gb_last_error() == -1
+    assert not lib.create_plan_2d_r2c(2, 8, 0)
+    lib.gb_clear_error()
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_valid_plan_without_gpu_reports_no_device(lib):
+    assert not lib.create_plan_1d_c2c(1024, K.FORWARD, 0)
+    assert lib.gb_last_error() == -3  # MUFFT_GB_ERR_NO_DEVICE
+    lib.gb_clear_error()
+
+
+def _sched(lib, N, kind, direction=K.FORWARD, flags=0, batch=1):
+    buf = C.create_string_buffer(4096)
+    rc = lib.gb_describe_schedule_1d(N, kind, direction, flags, batch, buf, 4096)
+    assert rc == 0, (rc, lib.gb_last_error_string())
+    return buf.value.decode()
+
+
+def test_single_pass_schedule(lib):
+    s = _sched(lib, 1024, 0, batch=4096)
+    assert s.count("tile") == 1 and "L=1024" in s and "grid=1024x1" in s
+    s = _sched(lib, 4096, 0, K.INVERSE)
+    assert "conj=3" in s
+    s = _sched(lib, 8192, 1, flags=K.FLAG_ZERO_PAD_UPPER_HALF)
+    assert "L=4096" in s and "+half" in s and "epi=r2c" in s
+    s = _sched(lib, 8192, 2)
+    assert "pro=c2r" in s
+
+
+def test_four_step_schedule(lib):
+    s = _sched(lib, 1 << 24, 0)
+    parts = s.split("; ")
+    assert len(parts) == 2
+    assert "L=4096" in parts[0] and "across/across" in parts[0] and "epi=twiddle" in parts[0]
+    assert "L=4096" in parts[1] and "along/across" in parts[1]
+    s = _sched(lib, 1 << 21, 1)  # r2c of 2^21 reals = 2^20 complex + in-place fix-up
+    assert s.split("; ")[-1].startswith("r2c_fixup")

@@ -1,0 +1,164 @@
+"""GPU tests of the extension API (mufft_gb300.h) and the memory contract:
+batched plans, stream execution on device buffers, error reporting, and the
+reference's alloc / convolve-func entry points."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import REL_L2_TOL, rel_l2
+from mufft_gb300 import capi as K
+from mufft_gb300 import signals
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import mufft_gb300
+    return mufft_gb300.load()
+
+
+@pytest.fixture(scope="module")
+def ora():
+    from oracle.oracle import load_oracle
+    return load_oracle()
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available()
+    return t
+
+
+def _dev(torch, arr):
+    return torch.from_numpy(np.ascontiguousarray(arr)).cuda()
+
+
+def _stream(torch):
+    return torch.cuda.current_stream().cuda_stream
+
+
+@pytest.mark.parametrize("N,B", [(1024, 4096), (4096, 257), (16, 1000), (2, 3), (16384, 17), (1 << 20, 3)])
+@pytest.mark.parametrize("direction", [K.FORWARD, K.INVERSE])
+def test_batched_c2c_device(gpu, ora, torch, N, B, direction):
+    x = signals.complex_uniform(20000 + N + B, N * B).reshape(B, N)
+    dx = _dev(torch, x)
+    dy = torch.empty_like(dx)
+    plan = gpu.gb_create_plan_1d_c2c_batched(N, direction, 0, B, 0, 0)
+    assert plan, gpu.gb_last_error_string()
+    try:
+        rc = gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch))
+        assert rc == 0, gpu.gb_last_error_string()
+        torch.cuda.synchronize()
+    finally:
+        gpu.free_plan_1d(plan)
+    got = dy.cpu().numpy()
+    rows = range(B) if B <= 8 else (0, 1, B // 2, B - 1)
+    want = ora.c2c_many(x[list(rows)], direction, 4)
+    for i, r in enumerate(rows):
+        assert rel_l2(got[r], want[i]) <= REL_L2_TOL, r
+
+
+def test_batched_strided_r2c_c2r(gpu, ora, torch):
+    N, B = 2048, 64
+    idist, odist = N + 64, N // 2 + 1 + 7   # padded layouts
+    x = np.zeros((B, idist), np.float32)
+    x[:, :N] = signals.uniform(21000, N * B).reshape(B, N)
+    dx = _dev(torch, x)
+    dX = torch.zeros((B, odist), dtype=torch.complex64, device="cuda")
+    plan = gpu.gb_create_plan_1d_r2c_batched(N, 0, B, idist, odist)
+    assert plan
+    assert gpu.gb_execute_plan_1d_async(plan, dX.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
+    torch.cuda.synchronize()
+    gpu.free_plan_1d(plan)
+    X = dX.cpu().numpy()
+    for r in (0, 31, 63):
+        assert rel_l2(X[r, : N // 2 + 1], ora.fft_r2c(x[r, :N])) <= REL_L2_TOL
+    # and back: c2r of the padded spectra into padded real rows
+    dy = torch.zeros((B, idist), dtype=torch.float32, device="cuda")
+    plan = gpu.gb_create_plan_1d_c2r_batched(N, 0, B, odist, idist)
+    assert plan
+    assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dX.data_ptr(), _stream(torch)) == 0
+    torch.cuda.synchronize()
+    gpu.free_plan_1d(plan)
+    y = dy.cpu().numpy()
+    assert rel_l2(y[:, :N] / N, x[:, :N]) < 1e-6
+    assert np.all(y[:, N:] == 0)  # padding untouched
+
+
+def test_sync_api_accepts_device_pointers(gpu, ora, torch):
+    N = 4096
+    x = signals.complex_uniform(22000, N)
+    dx = _dev(torch, x)
+    dy = torch.empty_like(dx)
+    plan = gpu.create_plan_1d_c2c(N, K.FORWARD, 0)
+    gpu.execute_plan_1d(plan, dy.data_ptr(), dx.data_ptr())
+    gpu.check("execute")
+    gpu.free_plan_1d(plan)
+    assert rel_l2(dy.cpu().numpy(), ora.fft_c2c(x, K.FORWARD)) <= REL_L2_TOL
+
+
+def test_async_rejects_host_pointers(gpu):
+    N = 256
+    x = np.zeros(N, np.complex64)
+    y = np.zeros(N, np.complex64)
+    plan = gpu.create_plan_1d_c2c(N, K.FORWARD, 0)
+    rc = gpu.gb_execute_plan_1d_async(plan, y.ctypes.data, x.ctypes.data, None)
+    assert rc == -4  # MUFFT_GB_ERR_HOST_POINTER
+    gpu.gb_clear_error()
+    gpu.free_plan_1d(plan)
+
+
+def test_alloc_contract(gpu):
+    p = gpu.alloc(1000)
+    assert p and p % 64 == 0
+    q = gpu.calloc(4096)
+    assert q and q % 64 == 0
+    assert bytes((C.c_char * 4096).from_address(q)) == b"\0" * 4096
+    # mufft_alloc memory works as transform input/output (pinned host memory)
+    N = 512
+    src = (C.c_float * (2 * N)).from_address(p if 1000 >= 8 * N else q)
+    gpu.free(p)
+    gpu.free(q)
+
+
+def test_pinned_buffers_round_trip(gpu, ora):
+    N = 8192
+    nbytes = N * 8
+    pin_in, pin_out = gpu.alloc(nbytes), gpu.alloc(nbytes)
+    x = signals.complex_uniform(23000, N)
+    C.memmove(pin_in, x.ctypes.data, nbytes)
+    plan = gpu.create_plan_1d_c2c(N, K.FORWARD, 0)
+    gpu.execute_plan_1d(plan, pin_out, pin_in)
+    gpu.check("execute")
+    gpu.free_plan_1d(plan)
+    y = np.empty(N, np.complex64)
+    C.memmove(y.ctypes.data, pin_out, nbytes)
+    gpu.free(pin_in)
+    gpu.free(pin_out)
+    assert rel_l2(y, ora.fft_c2c(x, K.FORWARD)) <= REL_L2_TOL
+
+
+def test_convolve_func(gpu, ora):
+    n = 1000
+    a = signals.complex_uniform(24000, n)
+    b = signals.complex_uniform(24001, n)
+    f = K.CONVOLVE_FUNC(gpu.get_convolve_func(0))
+    out = np.zeros(n, np.complex64)
+    f(out.ctypes.data, a.ctypes.data, b.ctypes.data, 0.25, n)
+    want = np.zeros(n, np.complex64)
+    ora.lib.oracle_convolve(want.ctypes.data, a.ctypes.data, b.ctypes.data, 0.25, n)
+    assert rel_l2(out, want) < 1e-6
+
+
+def test_plan_introspection(gpu):
+    plan = gpu.create_plan_1d_c2c(1 << 24, K.FORWARD, 0)
+    assert gpu.gb_plan_1d_launches(plan) == 2
+    buf = C.create_string_buffer(2048)
+    assert gpu.gb_plan_1d_describe(plan, buf, 2048) == 0
+    assert b"twiddle" in buf.value
+    gpu.free_plan_1d(plan)
