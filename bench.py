@@ -215,6 +215,9 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
     torch.cuda.set_device(local)
     lib = mufft_gb300.load()
     N, B, desc = WORKLOADS[args.workload]
+    if args.batch:
+        B = args.batch
+        desc += f" [batch overridden to {B}]"
     flops_step = 5.0 * N * math.log2(N) * B
     algo_bytes_pass = 16.0 * N * B  # each pass reads and writes every point once (complex64)
 
@@ -379,6 +382,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c_2^24")
+    ap.add_argument("--batch", type=int, default=0, help="override the workload's batch (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
