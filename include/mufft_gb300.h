@@ -87,6 +87,19 @@ int mufft_gb_plan_2d_describe(const mufft_plan_2d *plan, char *buf, size_t size)
 int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned flags, unsigned batch,
                                   char *buf, size_t size);
 
+/* ----------------------------------------------------------- tuning */
+
+/* Process-wide choice of the tile kernel used for transforms of length L
+ * whose loads / stores walk across neighbouring transforms (nonzero) or
+ * along one transform (zero): transforms_per_cta and elems_per_thread select
+ * among the compiled variants (mufft_gb_list_tiles; 0 = any), both 0
+ * restores the default.  Affects plans created afterwards. */
+int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_cta,
+                             unsigned elems_per_thread);
+/* Writes "L=.. R=.. C=.. along/across threads=.. smem=..; ..." for every
+ * compiled tile kernel; returns the full length. */
+int mufft_gb_list_tiles(char *buf, size_t size);
+
 /* ------------------------------------------------------ memory helpers */
 
 /* Device memory for callers that do not link the CUDA runtime themselves. */

@@ -104,12 +104,45 @@ static std::vector<TileKernel> &tile_table()
     return t;
 }
 
-const TileKernel *find_tile(int L, int lmap, int smap)
+static std::mutex g_choice_mu;
+static std::vector<TileKernel> g_choice;  // preferred (L, lmap, smap) -> C
+
+const TileKernel *find_tile(int L, int lmap, int smap, int C, int R)
 {
+    if (C == 0 && R == 0) {
+        std::lock_guard<std::mutex> lock(g_choice_mu);
+        for (const TileKernel &k : g_choice)
+            if (k.L == L && k.lmap == lmap && k.smap == smap) {
+                C = k.C;
+                R = k.R;
+            }
+    }
     for (const TileKernel &k : tile_table())
-        if (k.L == L && k.lmap == lmap && k.smap == smap)
+        if (k.L == L && k.lmap == lmap && k.smap == smap && (C == 0 || k.C == C) && (R == 0 || k.R == R))
             return &k;
     return nullptr;
+}
+
+bool set_tile_choice(int L, int lmap, int smap, int C, int R)
+{
+    if ((C != 0 || R != 0) && !find_tile(L, lmap, smap, C, R))
+        return false;
+    std::lock_guard<std::mutex> lock(g_choice_mu);
+    for (auto it = g_choice.begin(); it != g_choice.end(); ++it)
+        if (it->L == L && it->lmap == lmap && it->smap == smap) {
+            g_choice.erase(it);
+            break;
+        }
+    if (C != 0 || R != 0) {
+        TileKernel k{};
+        k.L = L;
+        k.lmap = lmap;
+        k.smap = smap;
+        k.C = C;
+        k.R = R;
+        g_choice.push_back(k);
+    }
+    return true;
 }
 
 }  // namespace mgb
@@ -122,7 +155,7 @@ constexpr int kMaxDevices = 64;
 
 struct DeviceState {
     bool ready = false;
-    float2 *tw = nullptr;  // exp(-2*pi*i*j/kMaxTile)
+    float2 *tw = nullptr;  // stage twiddle table (common.h: stage_table_base)
 };
 
 std::mutex g_dev_mu;
@@ -147,14 +180,22 @@ bool device_prepare(int *dev_out)
     std::lock_guard<std::mutex> lock(g_dev_mu);
     DeviceState &ds = g_dev[dev];
     if (!ds.ready) {
-        std::vector<float2> h(kMaxTile);
-        for (unsigned j = 0; j < kMaxTile; j++) {
-            double ph = -2.0 * M_PI * (double)j / (double)kMaxTile;
-            h[j] = make_float2((float)std::cos(ph), (float)std::sin(ph));
-        }
-        if (!cuda_ok(cudaMalloc(&ds.tw, kMaxTile * sizeof(float2)), "cudaMalloc(twiddles)"))
+        // W^(e*k) for e in {1, 2, 4, 8}, W = exp(-2*pi*i/(r*p)), FP64 then rounded
+        std::vector<float2> h(kStageTableFloat2);
+        const int radices[4] = {2, 4, 8, 16}, ps[3] = {16, 256, 4096};
+        for (int r : radices)
+            for (int p : ps) {
+                const long long n = (long long)r * p;
+                for (int k = 0; k < p; k++)
+                    for (int e = 0; e < 4; e++) {
+                        long long m = ((long long)(1 << e) * k) % n;
+                        double ph = -2.0 * M_PI * (double)m / (double)n;
+                        h[stage_table_base(r, p) + 4 * k + e] = make_float2((float)std::cos(ph), (float)std::sin(ph));
+                    }
+            }
+        if (!cuda_ok(cudaMalloc(&ds.tw, h.size() * sizeof(float2)), "cudaMalloc(twiddles)"))
             return false;
-        if (!cuda_ok(cudaMemcpy(ds.tw, h.data(), kMaxTile * sizeof(float2), cudaMemcpyHostToDevice),
+        if (!cuda_ok(cudaMemcpy(ds.tw, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice),
                      "cudaMemcpy(twiddles)"))
             return false;
         for (const TileKernel &k : tile_table()) {
@@ -248,6 +289,8 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
     for (size_t i = first; i < ps.size() && i - first < count; i++) {
         const Pass &p = ps[i];
         if (p.type == PASS_TILE) {
+            if ((p.k->lmap == ALONG && p.a.in_stride != 1) || (p.k->smap == ALONG && p.a.out_stride != 1))
+                return cudaErrorInvalidValue;  // ALONG phases assume unit stride
             TileArgs a = p.a;
             a.in = (const float2 *)pick(p.in_role, b);
             a.out = (float2 *)pick(p.out_role, b);
@@ -311,16 +354,13 @@ struct FftSpec {
 // Device tables and scratch a schedule needs; allocated unless `dry`.
 struct PlanResources {
     float2 *rtw = nullptr;
-    float2 *twA = nullptr, *twB = nullptr;
     float2 *scratch = nullptr;
     size_t scratch_bytes = 0;
     void release()
     {
         cudaFree(rtw);
-        cudaFree(twA);
-        cudaFree(twB);
         cudaFree(scratch);
-        rtw = twA = twB = scratch = nullptr;
+        rtw = scratch = nullptr;
     }
 };
 
@@ -376,23 +416,9 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
         set_error(MUFFT_GB_ERR_UNSUPPORTED, "no four-step kernels for %u x %u", N1, N2);
         return false;
     }
-    const unsigned twbits = (lg + 1) / 2;
     if (!dry) {
-        std::vector<float2> hb(1u << twbits), ha((M >> twbits) + 1);
-        for (size_t b = 0; b < hb.size(); b++) {
-            double ph = -2.0 * M_PI * (double)b / (double)M;
-            hb[b] = make_float2((float)std::cos(ph), (float)std::sin(ph));
-        }
-        for (size_t a = 0; a < ha.size(); a++) {
-            unsigned long long m = ((unsigned long long)a << twbits) % M;
-            double ph = -2.0 * M_PI * (double)m / (double)M;
-            ha[a] = make_float2((float)std::cos(ph), (float)std::sin(ph));
-        }
-        res.twA = upload(ha);
-        res.twB = upload(hb);
         res.scratch_bytes = (size_t)M * s.batch * sizeof(float2);
-        if (!res.twA || !res.twB ||
-            !cuda_ok(cudaMalloc(&res.scratch, res.scratch_bytes), "cudaMalloc(scratch)"))
+        if (!cuda_ok(cudaMalloc(&res.scratch, res.scratch_bytes), "cudaMalloc(scratch)"))
             return false;
     }
     Pass p1;
@@ -413,9 +439,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p1.a.mirror_len = M;
     p1.a.mirror_ldist = 1;
     p1.a.scale = s.scale;
-    p1.a.twA = res.twA;
-    p1.a.twB = res.twB;
-    p1.a.twbits = twbits;
+    p1.a.tw_scale = 2.0f / (float)M;
     p1.in_role = s.in_role;
     p1.in2_role = s.in2_role;
     p1.out_role = ROLE_SCRATCH;
@@ -1244,6 +1268,34 @@ int mufft_gb_device_synchronize(void)
     if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize"))
         return t_err;
     return MUFFT_GB_OK;
+}
+
+// ========================================================= tile choice
+
+int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_cta,
+                             unsigned elems_per_thread)
+{
+    if (!set_tile_choice((int)L, load_across ? ACROSS : ALONG, store_across ? ACROSS : ALONG,
+                         (int)transforms_per_cta, (int)elems_per_thread)) {
+        set_error(MUFFT_GB_ERR_INVALID, "no tile kernel L=%u C=%u R=%u for that map", L, transforms_per_cta,
+                  elems_per_thread);
+        return MUFFT_GB_ERR_INVALID;
+    }
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_list_tiles(char *buf, size_t size)
+{
+    std::string s;
+    char line[160];
+    for (const TileKernel &k : tile_table()) {
+        snprintf(line, sizeof(line), "%sL=%d R=%d C=%d %s/%s threads=%d smem=%zu", s.empty() ? "" : "; ", k.L, k.R,
+                 k.C, k.lmap ? "across" : "along", k.smap ? "across" : "along", k.threads, k.smem);
+        s += line;
+    }
+    if (buf && size)
+        snprintf(buf, size, "%s", s.c_str());
+    return (int)s.size();
 }
 
 // ================================================================ errors

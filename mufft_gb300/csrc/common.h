@@ -10,6 +10,20 @@ namespace mgb {
 constexpr unsigned kMaxTileLog2 = 14;
 constexpr unsigned kMaxTile = 1u << kMaxTileLog2;
 
+// Stage twiddle table.  A stage of radix r following sub-transforms of size p
+// (p in {16, 256, 4096} inside a tile) needs W^(m*k), W = exp(-2*pi*i/(r*p)),
+// for k < p and m < r.  For every (r, p) and k the table holds W^k, W^2k,
+// W^4k and W^8k as four consecutive float2 (32 bytes, two float4 loads); the
+// other powers are products of at most three of them.
+constexpr int kStageTableK = 16 + 256 + 4096;
+__host__ __device__ constexpr int stage_radix_index(int r) { return r == 2 ? 0 : r == 4 ? 1 : r == 8 ? 2 : 3; }
+__host__ __device__ constexpr int stage_p_offset(int p) { return p == 16 ? 0 : p == 256 ? 16 : 272; }
+__host__ __device__ constexpr int stage_table_base(int r, int p)
+{
+    return (stage_radix_index(r) * kStageTableK + stage_p_offset(p)) * 4;
+}
+constexpr int kStageTableFloat2 = 4 * kStageTableK * 4;
+
 // Thread-to-work decomposition of a CTA: which index runs fastest across
 // consecutive threads.  ALONG: consecutive threads walk along one transform
 // (contiguous rows); ACROSS: consecutive threads walk across neighbouring
@@ -46,7 +60,7 @@ struct TileArgs {
     int prologue;
     int half;                 // inputs n >= L/2 are zero and not read (MUFFT_FLAG_ZERO_PAD_UPPER_HALF)
     int epilogue;
-    const float2 *tw;         // exp(-2*pi*i*j/kMaxTile), j < kMaxTile
+    const float2 *tw;         // stage twiddle table (stage_table_base)
     // real<->complex fix-ups: twiddles of length M, mirror length M
     const float2 *rtw;
     long long mirror_len;     // M for PRO_C2R / PRO_MUL_C2R
@@ -54,10 +68,8 @@ struct TileArgs {
     // convolution prologues
     const float2 *in2;        // second spectrum (B)
     float scale;
-    // four-step twiddles: W_N^m = twA[m >> twbits] * twB[m & (2^twbits - 1)]
-    const float2 *twA;
-    const float2 *twB;
-    unsigned twbits;
+    // four-step twiddle W_N^m = exp(-2*pi*i*m/N): tw_scale = 2/N
+    float tw_scale;
 };
 
 }  // namespace mgb

@@ -153,8 +153,8 @@ template <int L, int R> struct Sched {
 
 // Shared-memory words per transform.  Positions are padded by one slot every
 // 16 (pos + pos/16) so that radix-16 strided writes spread over all banks; an
-// extra offset makes the region stride ≡ 32/C (mod 16) so that a warp walking
-// ACROSS C transforms also hits every bank pair at most twice.
+// extra offset makes the region stride ≡ 16/C (mod 16) so that the 16 lanes of
+// a half-warp walking ACROSS C transforms hit 16 distinct bank pairs.
 template <int L, int C, bool ACROSS_USED>
 __host__ __device__ constexpr int region_stride()
 {
@@ -163,7 +163,7 @@ __host__ __device__ constexpr int region_stride()
     int base = L + L / 16;
     if (!ACROSS_USED || C < 2)
         return base;
-    int want = (32 / C) % 16;
+    int want = C >= 16 ? 1 : 16 / C;  // 64-bit accesses are served per half-warp
     int have = base % 16;
     return base + ((want - have + 16) % 16);
 }
@@ -191,21 +191,42 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[R], int t, const float
 {
     using S = Sched<L, R>;
     constexpr int r = S::radix(s), p = S::pbefore(s), NB = R / r, T = S::T;
-    constexpr int F = (int)kMaxTile / (r * p);
 #pragma unroll
     for (int j = 0; j < NB; j++) {
-        if (p > 1) {
+        if constexpr (p > 1) {
             const int i = t + j * T;
             const int k = i & (p - 1);
+            const float4 *e = reinterpret_cast<const float4 *>(tw + stage_table_base(r, p) + 4 * k);
+            const float4 a = __ldg(e);
+            float2 w[16];
+            w[1] = make_float2(a.x, a.y);
+            w[2] = make_float2(a.z, a.w);
+            if constexpr (r > 4) {
+                const float4 b = __ldg(e + 1);
+                w[4] = make_float2(b.x, b.y);
+                w[8] = make_float2(b.z, b.w);
+            }
+            // remaining powers: at most three rounded products deep
+#pragma unroll
+            for (int m = 3; m < r; m++) {
+                if (m == 4 || m == 8)
+                    continue;
+                const int hi = m >= 8 ? 8 : (m >= 4 ? 4 : 2);
+                w[m] = cmul(w[m - hi], w[hi]);
+            }
 #pragma unroll
             for (int m = 1; m < r; m++)
-                v[j * r + m] = cmul(v[j * r + m], __ldg(&tw[m * k * F]));
+                v[j * r + m] = cmul(v[j * r + m], w[m]);
         }
         Dft<r>::run(&v[j * r]);
     }
 }
 
 // Store the outputs of stage s to the transform's shared-memory region.
+// Output m of butterfly i goes to (i - k)*r + k + m*p.  When p is a multiple
+// of 16 the padded address of that position is padpos(base) + m*(p + p/16),
+// and for p == 1, r == 16 it is 17*i + m, so the inner loop is a base plus
+// compile-time offsets.
 template <int L, int R, int s>
 __device__ __forceinline__ void stage_write(float2 *region, const float2 (&v)[R], int t)
 {
@@ -214,25 +235,48 @@ __device__ __forceinline__ void stage_write(float2 *region, const float2 (&v)[R]
 #pragma unroll
     for (int j = 0; j < NB; j++) {
         const int i = t + j * T;
-        const int k = i & (p - 1);
-        const int base = (i - k) * r + k;
+        if constexpr (p % 16 == 0) {
+            const int k = i & (p - 1);
+            float2 *b = region + padpos((i - k) * r + k);
 #pragma unroll
-        for (int m = 0; m < r; m++)
-            region[padpos(base + m * p)] = v[j * r + m];
+            for (int m = 0; m < r; m++)
+                b[m * (p + p / 16)] = v[j * r + m];
+        } else if constexpr (p == 1 && r == 16) {
+            float2 *b = region + 17 * i;
+#pragma unroll
+            for (int m = 0; m < r; m++)
+                b[m] = v[j * r + m];
+        } else {
+            const int k = i & (p - 1);
+            const int base = (i - k) * r + k;
+#pragma unroll
+            for (int m = 0; m < r; m++)
+                region[padpos(base + m * p)] = v[j * r + m];
+        }
     }
 }
 
-// Load the inputs of stage s from the transform's shared-memory region.
+// Load the inputs of stage s from the transform's shared-memory region:
+// register j*r + m <- position t + T*(j + m*NB).
 template <int L, int R, int s>
 __device__ __forceinline__ void stage_read(const float2 *region, float2 (&v)[R], int t)
 {
     using S = Sched<L, R>;
     constexpr int r = S::radix(s), NB = R / r, T = S::T;
+    if constexpr (T % 16 == 0) {
+        const float2 *b = region + padpos(t);
 #pragma unroll
-    for (int j = 0; j < NB; j++)
+        for (int j = 0; j < NB; j++)
 #pragma unroll
-        for (int m = 0; m < r; m++)
-            v[j * r + m] = region[padpos(t + T * (j + m * NB))];
+            for (int m = 0; m < r; m++)
+                v[j * r + m] = b[(j + m * NB) * (T + T / 16)];
+    } else {
+#pragma unroll
+        for (int j = 0; j < NB; j++)
+#pragma unroll
+            for (int m = 0; m < r; m++)
+                v[j * r + m] = region[padpos(t + T * (j + m * NB))];
+    }
 }
 
 // ------------------------------------------------------ prologue / epilogue
@@ -243,54 +287,96 @@ __device__ __forceinline__ float2 c2r_fixup(float2 a, float2 bm, float2 w)
     return cadd(cadd(a, b), cmul(csub(a, b), w));
 }
 
-// Stage-0 load: register j*r + m <- element t + T*(j + m*NB) of transform `tr`.
-template <int L, int R>
+// Stage-0 load: register j*r + m <- element t + T*(j + m*NB) of transform
+// `tr` (slot q = j + m*NB).  ALONG loads have unit stride (the planner only
+// builds them that way), so addresses are a base plus constant offsets.
+template <int L, int R, int LMAP>
 __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__restrict__ in,
                                             const float2 *__restrict__ in2, unsigned tr, int t,
                                             float2 (&v)[R])
 {
     using S = Sched<L, R>;
     constexpr int r = S::radix(0), NB = R / r, T = S::T;
-    const bool valid = tr < a.ntrans;
+#pragma unroll
+    for (int q = 0; q < R; q++)
+        v[q] = make_float2(0.f, 0.f);
+    if (tr >= a.ntrans)
+        return;
+    const int nq = a.half ? R / 2 : R;  // zero-padded upper half: slots q >= R/2 stay zero
     const long long tbase = (long long)tr * a.in_dist;
+    const long long step = (LMAP == ALONG) ? (long long)T : (long long)T * a.in_stride;
+    const long long first = tbase + ((LMAP == ALONG) ? (long long)t : (long long)t * a.in_stride);
+    switch (a.prologue) {
+    case PRO_PLAIN: {
+        const float2 *p0 = in + first;
 #pragma unroll
-    for (int j = 0; j < NB; j++) {
+        for (int j = 0; j < NB; j++)
 #pragma unroll
-        for (int m = 0; m < r; m++) {
-            const int pos = t + T * (j + m * NB);
-            float2 x = make_float2(0.f, 0.f);
-            if (valid && !(a.half && j + m * NB >= R / 2)) {
-                const long long addr = tbase + (long long)pos * a.in_stride;
-                switch (a.prologue) {
-                case PRO_C2R: {
-                    const long long local = (long long)tr * a.mirror_ldist + (long long)pos * a.in_stride;
-                    const long long tb = tbase - (long long)tr * a.mirror_ldist;
-                    x = c2r_fixup(__ldg(&in[tb + local]), __ldg(&in[tb + a.mirror_len - local]),
-                                  __ldg(&a.rtw[local]));
-                    break;
-                }
-                case PRO_MUL:
-                    x = cscale(cmul(__ldg(&in[addr]), __ldg(&in2[addr])), a.scale);
-                    break;
-                case PRO_MUL_C2R: {
-                    const long long local = (long long)tr * a.mirror_ldist + (long long)pos * a.in_stride;
-                    const long long tb = tbase - (long long)tr * a.mirror_ldist;
-                    const long long am = tb + local, bm = tb + a.mirror_len - local;
-                    float2 xa = cscale(cmul(__ldg(&in[am]), __ldg(&in2[am])), a.scale);
-                    float2 xb = cscale(cmul(__ldg(&in[bm]), __ldg(&in2[bm])), a.scale);
-                    x = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
-                    break;
-                }
-                default:
-                    x = __ldg(&in[addr]);
-                    break;
-                }
-                if (a.conj & 1)
-                    x = cconj(x);
+            for (int m = 0; m < r; m++) {
+                const int q = j + m * NB;
+                if (q < nq)
+                    v[j * r + m] = __ldg(p0 + q * step);
             }
-            v[j * r + m] = x;
-        }
+        break;
     }
+    case PRO_MUL: {
+        const float2 *p0 = in + first, *p1 = in2 + first;
+#pragma unroll
+        for (int j = 0; j < NB; j++)
+#pragma unroll
+            for (int m = 0; m < r; m++) {
+                const int q = j + m * NB;
+                if (q < nq)
+                    v[j * r + m] = cscale(cmul(__ldg(p0 + q * step), __ldg(p1 + q * step)), a.scale);
+            }
+        break;
+    }
+    default: {
+        // c2r fix-ups: X[local] and X[M - local] with local = tr*ldist + pos*stride
+        const long long tb = tbase - (long long)tr * a.mirror_ldist;
+        const long long lfirst = (long long)tr * a.mirror_ldist + (long long)t * a.in_stride;
+        const long long lstep = (long long)T * a.in_stride;
+        const bool mul = a.prologue == PRO_MUL_C2R;
+#pragma unroll
+        for (int j = 0; j < NB; j++)
+#pragma unroll
+            for (int m = 0; m < r; m++) {
+                const int q = j + m * NB;
+                if (q < nq) {
+                    const long long local = lfirst + q * lstep;
+                    const long long ia = tb + local, ib = tb + a.mirror_len - local;
+                    float2 xa = __ldg(&in[ia]), xb = __ldg(&in[ib]);
+                    if (mul) {
+                        xa = cscale(cmul(xa, __ldg(&in2[ia])), a.scale);
+                        xb = cscale(cmul(xb, __ldg(&in2[ib])), a.scale);
+                    }
+                    v[j * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
+                }
+            }
+        break;
+    }
+    }
+    if (a.conj & 1) {
+#pragma unroll
+        for (int q = 0; q < R; q++)
+            v[q].y = -v[q].y;
+    }
+}
+
+// W_N^m = exp(-2*pi*i*m/N) for m < N <= 2^28, scale = 2/N.  sincospif gets
+// an exactly representable argument: m itself when m < 2^24, otherwise the
+// product of the twiddles of m's high and low 12-bit parts.
+__device__ __forceinline__ float2 fourstep_twiddle(unsigned m, float scale)
+{
+    float s, c;
+    if (m < (1u << 24)) {
+        sincospif((float)m * scale, &s, &c);
+        return make_float2(c, -s);
+    }
+    float s2, c2;
+    sincospif((float)(m & ~4095u) * scale, &s, &c);
+    sincospif((float)(m & 4095u) * scale, &s2, &c2);
+    return cmul(make_float2(c, -s), make_float2(c2, -s2));
 }
 
 // Real-to-complex fix-up of bin k from Z[k] and Z[M-k] (kernel.c:47-82).
@@ -340,7 +426,7 @@ __global__ void __launch_bounds__(C *(L / R)) tile_fft(const TileArgs a)
     float2 v[R];
     int c, t;
     split_tid<LMAP, C, T>(threadIdx.x, c, t);
-    load_stage0<L, R>(a, in, in2, tile0 + c, t, v);
+    load_stage0<L, R, LMAP>(a, in, in2, tile0 + c, t, v);
     stage_compute<L, R, 0>(v, t, a.tw);
     run_stages<L, R, C, LMAP, SMAP, 1>(v, c, t, smem, a.tw);
 
@@ -400,21 +486,29 @@ __global__ void __launch_bounds__(C *(L / R)) tile_fft(const TileArgs a)
 
     if (!valid)
         return;
+    const long long ostep = (SMAP == ALONG) ? (long long)T : (long long)T * a.out_stride;
+    float2 *o0 = out + obase + ((SMAP == ALONG) ? (long long)t : (long long)t * a.out_stride);
+    if (a.epilogue == EPI_TWIDDLE) {
 #pragma unroll
-    for (int j = 0; j < NBL; j++) {
+        for (int j = 0; j < NBL; j++)
 #pragma unroll
-        for (int m = 0; m < rl; m++) {
-            const int pos = t + T * (j + m * NBL);
-            float2 y = v[j * rl + m];
-            if (a.epilogue == EPI_TWIDDLE) {
-                const unsigned mm = (unsigned)pos * tr;
-                const unsigned mask = (1u << a.twbits) - 1u;
-                y = cmul(y, cmul(__ldg(&a.twA[mm >> a.twbits]), __ldg(&a.twB[mm & mask])));
+            for (int m = 0; m < rl; m++) {
+                const int q = j + m * NBL;
+                float2 y = cmul(v[j * rl + m], fourstep_twiddle((unsigned)(t + T * q) * tr, a.tw_scale));
+                if (a.conj & 2)
+                    y.y = -y.y;
+                o0[q * ostep] = y;
             }
-            if (a.conj & 2)
-                y = cconj(y);
-            out[obase + (long long)pos * a.out_stride] = y;
-        }
+    } else {
+        const float sg = (a.conj & 2) ? -1.f : 1.f;
+#pragma unroll
+        for (int j = 0; j < NBL; j++)
+#pragma unroll
+            for (int m = 0; m < rl; m++) {
+                const int q = j + m * NBL;
+                const float2 y = v[j * rl + m];
+                o0[q * ostep] = make_float2(y.x, sg * y.y);
+            }
     }
 }
 

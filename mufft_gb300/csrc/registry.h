@@ -21,7 +21,10 @@ void register_tiles_along(std::vector<TileKernel> &out);
 void register_tiles_across(std::vector<TileKernel> &out);
 void register_tiles_transpose(std::vector<TileKernel> &out);
 
-// Returns the instantiation for (L, lmap, smap), or nullptr.
-const TileKernel *find_tile(int L, int lmap, int smap);
+// Returns the instantiation for (L, lmap, smap): the one with C transforms
+// per CTA when C > 0, else the preferred one (set_tile_choice) or the first
+// registered.  nullptr if none exists.
+const TileKernel *find_tile(int L, int lmap, int smap, int C = 0, int R = 0);
+bool set_tile_choice(int L, int lmap, int smap, int C, int R = 0);
 
 }  // namespace mgb

@@ -21,8 +21,13 @@ void register_tiles_across(std::vector<TileKernel> &out)
     TILE(256, 16, 16);
     TILE(512, 16, 8);
     TILE(1024, 16, 8);
+    TILE(1024, 16, 16);
     TILE(2048, 16, 4);
+    TILE(2048, 16, 8);
+    TILE(4096, 16, 4);  // default: measured fastest for the 4096 x 4096 four-step
+    TILE(4096, 16, 2);
     TILE(4096, 32, 4);
+    TILE(4096, 32, 2);
     TILE(8192, 32, 2);
     TILE(16384, 32, 1);
 }

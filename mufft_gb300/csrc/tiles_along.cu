@@ -22,7 +22,9 @@ void register_tiles_along(std::vector<TileKernel> &out)
     TILE(1024, 16, 4);
     TILE(2048, 16, 2);
     TILE(4096, 16, 1);
+    TILE(8192, 16, 1);
     TILE(8192, 32, 1);
+    TILE(16384, 16, 1);
     TILE(16384, 32, 1);
 }
 
