@@ -91,12 +91,13 @@ int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned 
 
 /* Process-wide choice of the tile kernel used for transforms of length L
  * whose loads / stores walk across neighbouring transforms (nonzero) or
- * along one transform (zero): transforms_per_cta and elems_per_thread select
- * among the compiled variants (mufft_gb_list_tiles; 0 = any), both 0
- * restores the default.  Affects plans created afterwards. */
-int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_cta,
-                             unsigned elems_per_thread);
-/* Writes "L=.. R=.. C=.. along/across threads=.. smem=..; ..." for every
+ * along one transform (zero): transforms_per_tile, elems_per_thread and
+ * cluster_ctas (CTAs a tile is spread over) select among the compiled
+ * variants (mufft_gb_list_tiles; 0 = any); all three 0 restores the default.
+ * Affects plans created afterwards. */
+int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_tile,
+                             unsigned elems_per_thread, unsigned cluster_ctas);
+/* Writes "L=.. R=.. C=.. Q=.. along/across threads=.. smem=..; ..." for every
  * compiled tile kernel; returns the full length. */
 int mufft_gb_list_tiles(char *buf, size_t size);
 

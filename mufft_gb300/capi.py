@@ -78,7 +78,7 @@ GB_H = [
     ("plan_1d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("plan_2d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, C.c_char_p, _sz]),
-    ("set_tile_choice", _i, [_u, _i, _i, _u, _u]),
+    ("set_tile_choice", _i, [_u, _i, _i, _u, _u, _u]),
     ("list_tiles", _i, [C.c_char_p, _sz]),
     ("device_alloc", _vp, [_sz]),
     ("device_free", None, [_vp]),

@@ -107,25 +107,27 @@ static std::vector<TileKernel> &tile_table()
 static std::mutex g_choice_mu;
 static std::vector<TileKernel> g_choice;  // preferred (L, lmap, smap) -> C
 
-const TileKernel *find_tile(int L, int lmap, int smap, int C, int R)
+const TileKernel *find_tile(int L, int lmap, int smap, int C, int R, int Q)
 {
-    if (C == 0 && R == 0) {
+    if (C == 0 && R == 0 && Q == 0) {
         std::lock_guard<std::mutex> lock(g_choice_mu);
         for (const TileKernel &k : g_choice)
             if (k.L == L && k.lmap == lmap && k.smap == smap) {
                 C = k.C;
                 R = k.R;
+                Q = k.Q;
             }
     }
     for (const TileKernel &k : tile_table())
-        if (k.L == L && k.lmap == lmap && k.smap == smap && (C == 0 || k.C == C) && (R == 0 || k.R == R))
+        if (k.L == L && k.lmap == lmap && k.smap == smap && (C == 0 || k.C == C) && (R == 0 || k.R == R) &&
+            (Q == 0 || k.Q == Q))
             return &k;
     return nullptr;
 }
 
-bool set_tile_choice(int L, int lmap, int smap, int C, int R)
+bool set_tile_choice(int L, int lmap, int smap, int C, int R, int Q)
 {
-    if ((C != 0 || R != 0) && !find_tile(L, lmap, smap, C, R))
+    if ((C != 0 || R != 0 || Q != 0) && !find_tile(L, lmap, smap, C, R, Q))
         return false;
     std::lock_guard<std::mutex> lock(g_choice_mu);
     for (auto it = g_choice.begin(); it != g_choice.end(); ++it)
@@ -133,13 +135,14 @@ bool set_tile_choice(int L, int lmap, int smap, int C, int R)
             g_choice.erase(it);
             break;
         }
-    if (C != 0 || R != 0) {
+    if (C != 0 || R != 0 || Q != 0) {
         TileKernel k{};
         k.L = L;
         k.lmap = lmap;
         k.smap = smap;
         k.C = C;
         k.R = R;
+        k.Q = Q;
         g_choice.push_back(k);
     }
     return true;
@@ -296,7 +299,25 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             a.out = (float2 *)pick(p.out_role, b);
             a.in2 = (const float2 *)pick(p.in2_role, b);
             void *args[] = {&a};
-            cudaError_t e = cudaLaunchKernel(p.k->fn, p.grid, dim3(p.k->threads), args, p.k->smem, st);
+            cudaError_t e;
+            if (p.k->Q > 1) {
+                // one tile per cluster of Q CTAs (distributed shared memory)
+                cudaLaunchConfig_t cfg = {};
+                cudaLaunchAttribute attr[1];
+                cfg.gridDim = dim3(p.grid.x * p.k->Q, p.grid.y, p.grid.z);
+                cfg.blockDim = dim3(p.k->threads);
+                cfg.dynamicSmemBytes = p.k->smem;
+                cfg.stream = st;
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = p.k->Q;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                e = cudaLaunchKernelExC(&cfg, p.k->fn, args);
+            } else {
+                e = cudaLaunchKernel(p.k->fn, p.grid, dim3(p.k->threads), args, p.k->smem, st);
+            }
             if (e != cudaSuccess)
                 return e;
         } else {
@@ -327,8 +348,8 @@ std::string describe(const std::vector<Pass> &ps)
     for (size_t i = 0; i < ps.size(); i++) {
         const Pass &p = ps[i];
         if (p.type == PASS_TILE)
-            snprintf(buf, sizeof(buf), "%stile L=%d R=%d C=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s conj=%d",
-                     i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->lmap ? "across" : "along",
+            snprintf(buf, sizeof(buf), "%stile L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s conj=%d",
+                     i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue), p.a.conj);
         else
@@ -369,7 +390,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
 {
     const unsigned M = s.M;
     const bool r2c = s.epilogue == EPI_R2C || s.epilogue == EPI_R2C_FULL;
-    if (M <= kMaxTile) {
+    if (M <= kMaxSinglePass) {
         const TileKernel *k = find_tile((int)M, ALONG, ALONG);
         if (!k) {
             set_error(MUFFT_GB_ERR_UNSUPPORTED, "no tile kernel for length %u", M);
@@ -1012,8 +1033,8 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         return nullptr;
     }
     const unsigned Mx = kind == K2_C2C ? Nx : Nx / 2;
-    if (Mx > kMaxTile || Ny > kMaxTile) {
-        set_error(MUFFT_GB_ERR_UNSUPPORTED, "2D side longer than %u", kMaxTile);
+    if (Mx > kMaxSinglePass || Ny > kMaxSinglePass) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "2D side longer than %u", kMaxSinglePass);
         return nullptr;
     }
     const TileKernel *krow = find_tile((int)Mx, ALONG, ALONG);
@@ -1272,13 +1293,13 @@ int mufft_gb_device_synchronize(void)
 
 // ========================================================= tile choice
 
-int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_cta,
-                             unsigned elems_per_thread)
+int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_tile,
+                             unsigned elems_per_thread, unsigned cluster_ctas)
 {
     if (!set_tile_choice((int)L, load_across ? ACROSS : ALONG, store_across ? ACROSS : ALONG,
-                         (int)transforms_per_cta, (int)elems_per_thread)) {
-        set_error(MUFFT_GB_ERR_INVALID, "no tile kernel L=%u C=%u R=%u for that map", L, transforms_per_cta,
-                  elems_per_thread);
+                         (int)transforms_per_tile, (int)elems_per_thread, (int)cluster_ctas)) {
+        set_error(MUFFT_GB_ERR_INVALID, "no tile kernel L=%u C=%u R=%u Q=%u for that map", L, transforms_per_tile,
+                  elems_per_thread, cluster_ctas);
         return MUFFT_GB_ERR_INVALID;
     }
     return MUFFT_GB_OK;
@@ -1289,8 +1310,8 @@ int mufft_gb_list_tiles(char *buf, size_t size)
     std::string s;
     char line[160];
     for (const TileKernel &k : tile_table()) {
-        snprintf(line, sizeof(line), "%sL=%d R=%d C=%d %s/%s threads=%d smem=%zu", s.empty() ? "" : "; ", k.L, k.R,
-                 k.C, k.lmap ? "across" : "along", k.smap ? "across" : "along", k.threads, k.smem);
+        snprintf(line, sizeof(line), "%sL=%d R=%d C=%d Q=%d %s/%s threads=%d smem=%zu", s.empty() ? "" : "; ", k.L,
+                 k.R, k.C, k.Q, k.lmap ? "across" : "along", k.smap ? "across" : "along", k.threads, k.smem);
         s += line;
     }
     if (buf && size)

@@ -6,9 +6,14 @@
 
 namespace mgb {
 
-// Largest FFT length one CTA keeps on chip (registers + shared memory).
-constexpr unsigned kMaxTileLog2 = 14;
+// Largest FFT length a tile can hold on chip (shared memory of a cluster of
+// up to 8 CTAs), and the largest the planner runs as a single pass by
+// default: beyond 16384 the four-step path measured faster on GB300 than
+// cluster tiles, whose stage exchanges are bound by distributed-shared-memory
+// bandwidth.
+constexpr unsigned kMaxTileLog2 = 16;
 constexpr unsigned kMaxTile = 1u << kMaxTileLog2;
+constexpr unsigned kMaxSinglePass = 16384;
 
 // Stage twiddle table.  A stage of radix r following sub-transforms of size p
 // (p in {16, 256, 4096} inside a tile) needs W^(m*k), W = exp(-2*pi*i/(r*p)),

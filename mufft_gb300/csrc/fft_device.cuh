@@ -15,9 +15,13 @@
 // read and one write pass over HBM.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "common.h"
 
 namespace mgb {
+
+namespace cg = cooperative_groups;
 
 // ------------------------------------------------------------ complex math
 
@@ -136,7 +140,6 @@ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
 template <int L, int R> struct Sched {
     static_assert(L >= 2 && (L & (L - 1)) == 0, "power of two");
     static_assert(R <= L && L % R == 0, "R divides L");
-    static constexpr int T = L / R;                  // threads per transform
     static constexpr int LOG = ilog2c(L);
     static constexpr int NFULL = L < 16 ? 0 : LOG / 4;
     static constexpr int REMB = L < 16 ? LOG : LOG % 4;
@@ -151,19 +154,44 @@ template <int L, int R> struct Sched {
     }
 };
 
-// Shared-memory words per transform.  Positions are padded by one slot every
-// 16 (pos + pos/16) so that radix-16 strided writes spread over all banks; an
-// extra offset makes the region stride ≡ 16/C (mod 16) so that the 16 lanes of
-// a half-warp walking ACROSS C transforms hit 16 distinct bank pairs.
-template <int L, int C, bool ACROSS_USED>
+// A tile is C transforms of length L spread over a cluster of Q CTAs: CTA
+// rank j owns positions [j*L/Q, (j+1)*L/Q) of every transform in its shared
+// memory and, in stage s (radix r), butterflies [j*B, (j+1)*B) with
+// B = L/(r*Q).  Thread tl of a transform runs butterflies j*B + tl + TL*u,
+// u < R/r.  When B is a multiple of the stage's sub-transform size p, the
+// outputs (i - k)*r + k + m*p of those butterflies fall in the CTA's own
+// slice, so every stage writes locally and reads its inputs i + m*L/r from
+// whichever CTA owns them (distributed shared memory when Q > 1).
+template <int L, int R, int Q> struct Tile {
+    using S = Sched<L, R>;
+    static constexpr int TL = L / (R * Q);  // threads per transform per CTA
+    static constexpr int LQ = L / Q;        // positions per CTA per transform
+    static_assert(TL >= 1 && L % (R * Q) == 0, "R*Q must divide L");
+    __host__ __device__ static constexpr int B(int s) { return L / (S::radix(s) * Q); }
+    __host__ __device__ static constexpr bool local_writes()
+    {
+        for (int s = 0; s + 1 < S::NST; s++)
+            if (B(s) % S::pbefore(s) != 0)
+                return false;
+        return true;
+    }
+    static_assert(Q == 1 || local_writes(), "stage outputs must stay in the writing CTA");
+};
+
+// Shared-memory words per transform slice.  Positions are padded by one slot
+// every 16 (pos + pos/16) so that radix-16 strided writes spread over all
+// banks; an extra offset makes the slice stride ≡ 16/C (mod 16) so that the
+// 16 lanes of a half-warp walking ACROSS C transforms hit 16 distinct bank
+// pairs (64-bit accesses are served per half-warp).
+template <int LQ, int C, bool ACROSS_USED>
 __host__ __device__ constexpr int region_stride()
 {
-    if (L < 16)
-        return L;
-    int base = L + L / 16;
+    if (LQ < 16)
+        return LQ;
+    int base = LQ + LQ / 16;
     if (!ACROSS_USED || C < 2)
         return base;
-    int want = C >= 16 ? 1 : 16 / C;  // 64-bit accesses are served per half-warp
+    int want = C >= 16 ? 1 : 16 / C;
     int have = base % 16;
     return base + ((want - have + 16) % 16);
 }
@@ -182,19 +210,29 @@ __device__ __forceinline__ void split_tid(int tid, int &c, int &t)
     }
 }
 
+template <int Q>
+__device__ __forceinline__ void tile_sync()
+{
+    if constexpr (Q > 1)
+        cg::this_cluster().sync();
+    else
+        __syncthreads();
+}
+
 // ---------------------------------------------------------------- stages
 
 // Twiddle multiply and DFT of stage s on the thread's R registers.
-// Register j*r + m holds input m of butterfly i = t + j*T.
-template <int L, int R, int s>
-__device__ __forceinline__ void stage_compute(float2 (&v)[R], int t, const float2 *__restrict__ tw)
+// Register u*r + m holds input m of butterfly i = j*B + tl + TL*u.
+template <int L, int R, int Q, int s>
+__device__ __forceinline__ void stage_compute(float2 (&v)[R], int j, int tl, const float2 *__restrict__ tw)
 {
     using S = Sched<L, R>;
-    constexpr int r = S::radix(s), p = S::pbefore(s), NB = R / r, T = S::T;
+    using TT = Tile<L, R, Q>;
+    constexpr int r = S::radix(s), p = S::pbefore(s), NB = R / r;
 #pragma unroll
-    for (int j = 0; j < NB; j++) {
+    for (int u = 0; u < NB; u++) {
         if constexpr (p > 1) {
-            const int i = t + j * T;
+            const int i = j * TT::B(s) + tl + TT::TL * u;
             const int k = i & (p - 1);
             const float4 *e = reinterpret_cast<const float4 *>(tw + stage_table_base(r, p) + 4 * k);
             const float4 a = __ldg(e);
@@ -216,66 +254,85 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[R], int t, const float
             }
 #pragma unroll
             for (int m = 1; m < r; m++)
-                v[j * r + m] = cmul(v[j * r + m], w[m]);
+                v[u * r + m] = cmul(v[u * r + m], w[m]);
         }
-        Dft<r>::run(&v[j * r]);
+        Dft<r>::run(&v[u * r]);
     }
 }
 
-// Store the outputs of stage s to the transform's shared-memory region.
-// Output m of butterfly i goes to (i - k)*r + k + m*p.  When p is a multiple
-// of 16 the padded address of that position is padpos(base) + m*(p + p/16),
-// and for p == 1, r == 16 it is 17*i + m, so the inner loop is a base plus
-// compile-time offsets.
-template <int L, int R, int s>
-__device__ __forceinline__ void stage_write(float2 *region, const float2 (&v)[R], int t)
+// Store the outputs of stage s into the CTA's own slice (local offset
+// pos - j*LQ).  Output m of butterfly i goes to (i - k)*r + k + m*p; when p
+// is a multiple of 16 the padded address is padpos(base) + m*(p + p/16), and
+// for p == 1, r == 16 it is 17*(i - j*LQ/16) + m: a base plus constants.
+template <int L, int R, int Q, int s>
+__device__ __forceinline__ void stage_write(float2 *region, const float2 (&v)[R], int j, int tl)
 {
     using S = Sched<L, R>;
-    constexpr int r = S::radix(s), p = S::pbefore(s), NB = R / r, T = S::T;
+    using TT = Tile<L, R, Q>;
+    constexpr int r = S::radix(s), p = S::pbefore(s), NB = R / r;
 #pragma unroll
-    for (int j = 0; j < NB; j++) {
-        const int i = t + j * T;
+    for (int u = 0; u < NB; u++) {
+        const int i = j * TT::B(s) + tl + TT::TL * u;
         if constexpr (p % 16 == 0) {
             const int k = i & (p - 1);
-            float2 *b = region + padpos((i - k) * r + k);
+            float2 *b = region + padpos((i - k) * r + k - j * TT::LQ);
 #pragma unroll
             for (int m = 0; m < r; m++)
-                b[m * (p + p / 16)] = v[j * r + m];
+                b[m * (p + p / 16)] = v[u * r + m];
         } else if constexpr (p == 1 && r == 16) {
-            float2 *b = region + 17 * i;
+            float2 *b = region + 17 * (i - j * (TT::LQ / 16));
 #pragma unroll
             for (int m = 0; m < r; m++)
-                b[m] = v[j * r + m];
+                b[m] = v[u * r + m];
         } else {
             const int k = i & (p - 1);
-            const int base = (i - k) * r + k;
+            const int base = (i - k) * r + k - j * TT::LQ;
 #pragma unroll
             for (int m = 0; m < r; m++)
-                region[padpos(base + m * p)] = v[j * r + m];
+                region[padpos(base + m * p)] = v[u * r + m];
         }
     }
 }
 
-// Load the inputs of stage s from the transform's shared-memory region:
-// register j*r + m <- position t + T*(j + m*NB).
-template <int L, int R, int s>
-__device__ __forceinline__ void stage_read(const float2 *region, float2 (&v)[R], int t)
+// Load the inputs of stage s: register u*r + m <- position i + m*L/r, which
+// is local offset B*((j + m*Q) % r) + tl + TL*u in the slice of CTA
+// (j + m*Q) / r.
+template <int L, int R, int Q, int s>
+__device__ __forceinline__ void stage_read(float2 *region, float2 (&v)[R], int j, int tl)
 {
     using S = Sched<L, R>;
-    constexpr int r = S::radix(s), NB = R / r, T = S::T;
-    if constexpr (T % 16 == 0) {
-        const float2 *b = region + padpos(t);
+    using TT = Tile<L, R, Q>;
+    constexpr int r = S::radix(s), NB = R / r, B = TT::B(s), TL = TT::TL;
+    if constexpr (Q == 1 && TL % 16 == 0 && B % 16 == 0) {
+        const float2 *b = region + padpos(tl);
 #pragma unroll
-        for (int j = 0; j < NB; j++)
+        for (int u = 0; u < NB; u++)
 #pragma unroll
             for (int m = 0; m < r; m++)
-                v[j * r + m] = b[(j + m * NB) * (T + T / 16)];
+                v[u * r + m] = b[(B * m + TL * u) / 16 * 17];
+    } else if constexpr (TL % 16 == 0 && B % 16 == 0 && r % Q == 0) {
+        // Q divides r and j < Q: input m lives in CTA (m*Q)/r at local offset
+        // B*j + B*((m*Q) % r) + tl + TL*u -- compile-time owners and offsets.
+        const int lbase = padpos(B * j + tl);
+#pragma unroll
+        for (int m = 0; m < r; m++) {
+            const int owner = (m * Q) / r;
+            const int lq = (m * Q) % r;
+            const float2 *b = cg::this_cluster().map_shared_rank(region, owner) + lbase + B * lq + B * lq / 16;
+#pragma unroll
+            for (int u = 0; u < NB; u++)
+                v[u * r + m] = b[TL * u + TL * u / 16];
+        }
     } else {
 #pragma unroll
-        for (int j = 0; j < NB; j++)
+        for (int m = 0; m < r; m++) {
+            const int owner = (j + m * Q) / r;
+            const int lq = (j + m * Q) % r;
+            const float2 *b = Q > 1 ? cg::this_cluster().map_shared_rank(region, owner) : region;
 #pragma unroll
-            for (int m = 0; m < r; m++)
-                v[j * r + m] = region[padpos(t + T * (j + m * NB))];
+            for (int u = 0; u < NB; u++)
+                v[u * r + m] = b[padpos(B * lq + tl + TL * u)];
+        }
     }
 }
 
@@ -287,72 +344,68 @@ __device__ __forceinline__ float2 c2r_fixup(float2 a, float2 bm, float2 w)
     return cadd(cadd(a, b), cmul(csub(a, b), w));
 }
 
-// Stage-0 load: register j*r + m <- element t + T*(j + m*NB) of transform
-// `tr` (slot q = j + m*NB).  ALONG loads have unit stride (the planner only
-// builds them that way), so addresses are a base plus constant offsets.
-template <int L, int R, int LMAP>
+// Stage-0 load: register u*r + m <- element p = j*B + tl + TL*u + m*Q*B of
+// transform `tr`.  ALONG loads have unit stride (the planner only builds them
+// that way), so addresses are a base plus constant offsets.
+template <int L, int R, int Q, int LMAP>
 __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__restrict__ in,
-                                            const float2 *__restrict__ in2, unsigned tr, int t,
+                                            const float2 *__restrict__ in2, unsigned tr, int j, int tl,
                                             float2 (&v)[R])
 {
     using S = Sched<L, R>;
-    constexpr int r = S::radix(0), NB = R / r, T = S::T;
+    using TT = Tile<L, R, Q>;
+    constexpr int r = S::radix(0), NB = R / r, B = TT::B(0), TL = TT::TL;
 #pragma unroll
     for (int q = 0; q < R; q++)
         v[q] = make_float2(0.f, 0.f);
     if (tr >= a.ntrans)
         return;
-    const int nq = a.half ? R / 2 : R;  // zero-padded upper half: slots q >= R/2 stay zero
+    const int mlim = a.half ? r / 2 : r;  // zero-padded upper half: inputs m >= r/2 stay zero
     const long long tbase = (long long)tr * a.in_dist;
-    const long long step = (LMAP == ALONG) ? (long long)T : (long long)T * a.in_stride;
-    const long long first = tbase + ((LMAP == ALONG) ? (long long)t : (long long)t * a.in_stride);
+    const long long p0 = (long long)j * B + tl;  // position of register 0
+    const long long sst = (LMAP == ALONG) ? 1 : a.in_stride;
+    const float2 *f = in + tbase + p0 * sst;
     switch (a.prologue) {
     case PRO_PLAIN: {
-        const float2 *p0 = in + first;
 #pragma unroll
-        for (int j = 0; j < NB; j++)
+        for (int u = 0; u < NB; u++)
 #pragma unroll
-            for (int m = 0; m < r; m++) {
-                const int q = j + m * NB;
-                if (q < nq)
-                    v[j * r + m] = __ldg(p0 + q * step);
-            }
+            for (int m = 0; m < r; m++)
+                if (m < mlim)
+                    v[u * r + m] = __ldg(f + (long long)(TL * u + m * Q * B) * sst);
         break;
     }
     case PRO_MUL: {
-        const float2 *p0 = in + first, *p1 = in2 + first;
+        const float2 *g = in2 + tbase + p0 * sst;
 #pragma unroll
-        for (int j = 0; j < NB; j++)
+        for (int u = 0; u < NB; u++)
 #pragma unroll
-            for (int m = 0; m < r; m++) {
-                const int q = j + m * NB;
-                if (q < nq)
-                    v[j * r + m] = cscale(cmul(__ldg(p0 + q * step), __ldg(p1 + q * step)), a.scale);
-            }
+            for (int m = 0; m < r; m++)
+                if (m < mlim) {
+                    const long long o = (long long)(TL * u + m * Q * B) * sst;
+                    v[u * r + m] = cscale(cmul(__ldg(f + o), __ldg(g + o)), a.scale);
+                }
         break;
     }
     default: {
         // c2r fix-ups: X[local] and X[M - local] with local = tr*ldist + pos*stride
         const long long tb = tbase - (long long)tr * a.mirror_ldist;
-        const long long lfirst = (long long)tr * a.mirror_ldist + (long long)t * a.in_stride;
-        const long long lstep = (long long)T * a.in_stride;
+        const long long lfirst = (long long)tr * a.mirror_ldist + p0 * a.in_stride;
         const bool mul = a.prologue == PRO_MUL_C2R;
 #pragma unroll
-        for (int j = 0; j < NB; j++)
+        for (int u = 0; u < NB; u++)
 #pragma unroll
-            for (int m = 0; m < r; m++) {
-                const int q = j + m * NB;
-                if (q < nq) {
-                    const long long local = lfirst + q * lstep;
+            for (int m = 0; m < r; m++)
+                if (m < mlim) {
+                    const long long local = lfirst + (long long)(TL * u + m * Q * B) * a.in_stride;
                     const long long ia = tb + local, ib = tb + a.mirror_len - local;
                     float2 xa = __ldg(&in[ia]), xb = __ldg(&in[ib]);
                     if (mul) {
                         xa = cscale(cmul(xa, __ldg(&in2[ia])), a.scale);
                         xb = cscale(cmul(xb, __ldg(&in2[ib])), a.scale);
                     }
-                    v[j * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
+                    v[u * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
                 }
-            }
         break;
     }
     }
@@ -391,81 +444,116 @@ __device__ __forceinline__ void r2c_bins(float2 zk, float2 zmk, float2 w, float2
 
 // --------------------------------------------------------------- kernel
 
-template <int L, int R, int C, int LMAP, int SMAP, int s>
-__device__ __forceinline__ void run_stages(float2 (&v)[R], int &c, int &t, float2 *smem,
+template <int L, int R, int C, int Q, int LMAP, int SMAP, int s>
+__device__ __forceinline__ void run_stages(float2 (&v)[R], int j, int &c, int &tl, float2 *smem,
                                            const float2 *__restrict__ tw)
 {
     using S = Sched<L, R>;
+    using TT = Tile<L, R, Q>;
     if constexpr (s < S::NST) {
-        constexpr int RS = region_stride<L, C, (LMAP == ACROSS || SMAP == ACROSS)>();
-        stage_write<L, R, s - 1>(smem + c * RS, v, t);
-        __syncthreads();
-        split_tid<(s == S::NST - 1) ? SMAP : ALONG, C, S::T>(threadIdx.x, c, t);
-        stage_read<L, R, s>(smem + c * RS, v, t);
+        constexpr int RS = region_stride<TT::LQ, C, (LMAP == ACROSS || SMAP == ACROSS)>();
+        stage_write<L, R, Q, s - 1>(smem + c * RS, v, j, tl);
+        tile_sync<Q>();
+        split_tid<(s == S::NST - 1) ? SMAP : ALONG, C, TT::TL>(threadIdx.x, c, tl);
+        stage_read<L, R, Q, s>(smem + c * RS, v, j, tl);
         if (s < S::NST - 1)
-            __syncthreads();
-        stage_compute<L, R, s>(v, t, tw);
-        run_stages<L, R, C, LMAP, SMAP, s + 1>(v, c, t, smem, tw);
+            tile_sync<Q>();
+        stage_compute<L, R, Q, s>(v, j, tl, tw);
+        run_stages<L, R, C, Q, LMAP, SMAP, s + 1>(v, j, c, tl, smem, tw);
     }
 }
 
-template <int L, int R, int C, int LMAP, int SMAP>
-__global__ void __launch_bounds__(C *(L / R)) tile_fft(const TileArgs a)
+// Threads of one CTA, and the CTAs per SM the register budget is sized for:
+// 16-element tiles are held to 64 registers so that 2048 threads fit.
+template <int L, int R, int C, int Q> constexpr int tile_threads() { return C * (L / (R * Q)); }
+template <int L, int R, int C, int Q> constexpr int tile_min_blocks()
+{
+    return R <= 16 ? (tile_threads<L, R, C, Q>() >= 1024 ? 1 : 1024 / tile_threads<L, R, C, Q>()) : 1;
+}
+
+template <int L, int R, int C, int Q, int LMAP, int SMAP>
+__global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L, R, C, Q>()) tile_fft(const TileArgs a)
 {
     using S = Sched<L, R>;
-    constexpr int T = S::T, NST = S::NST;
-    constexpr int RS = region_stride<L, C, (LMAP == ACROSS || SMAP == ACROSS)>();
+    using TT = Tile<L, R, Q>;
+    constexpr int TL = TT::TL, NST = S::NST;
+    constexpr int RS = region_stride<TT::LQ, C, (LMAP == ACROSS || SMAP == ACROSS)>();
     static_assert(NST > 1 || LMAP == SMAP, "single-stage tiles cannot change the thread map");
+    static_assert(NST > 1 || Q == 1, "single-stage tiles are not split over a cluster");
     extern __shared__ float2 smem[];
 
     const float2 *in = a.in + (long long)blockIdx.y * a.in_batch;
     const float2 *in2 = a.in2 ? a.in2 + (long long)blockIdx.y * a.in_batch : nullptr;
     float2 *out = a.out + (long long)blockIdx.y * a.out_batch;
-    const unsigned tile0 = blockIdx.x * C;
+    int j = 0;
+    unsigned tile = blockIdx.x;
+    if constexpr (Q > 1) {
+        j = (int)cg::this_cluster().block_rank();
+        tile = blockIdx.x / Q;
+    }
+    const unsigned tile0 = tile * C;
 
     float2 v[R];
-    int c, t;
-    split_tid<LMAP, C, T>(threadIdx.x, c, t);
-    load_stage0<L, R, LMAP>(a, in, in2, tile0 + c, t, v);
-    stage_compute<L, R, 0>(v, t, a.tw);
-    run_stages<L, R, C, LMAP, SMAP, 1>(v, c, t, smem, a.tw);
+    int c, tl;
+    split_tid<LMAP, C, TL>(threadIdx.x, c, tl);
+    load_stage0<L, R, Q, LMAP>(a, in, in2, tile0 + c, j, tl, v);
+    stage_compute<L, R, Q, 0>(v, j, tl, a.tw);
+    run_stages<L, R, C, Q, LMAP, SMAP, 1>(v, j, c, tl, smem, a.tw);
+    // No CTA of the cluster may leave while others still read its slice.
+    if constexpr (Q > 1)
+        cg::this_cluster().barrier_arrive();
 
-    // Last stage: register j*r + m holds output t + T*(j + m*NB).
-    constexpr int rl = S::radix(NST - 1), NBL = R / rl;
+    // Last stage: register u*rl + m holds output p = j*B + tl + TL*u + m*Q*B.
+    constexpr int rl = S::radix(NST - 1), NBL = R / rl, BL = TT::B(NST - 1);
     const unsigned tr = tile0 + c;
     const bool valid = tr < a.ntrans;
     const long long obase = (long long)tr * a.out_dist;
+    const int p0 = j * BL + tl;
 
     if (a.epilogue == EPI_R2C || a.epilogue == EPI_R2C_FULL) {
-        // Z[k] and Z[L-k] sit in different threads: go through shared memory.
-        constexpr int M = L;
+        // Z[k] and Z[L-k] sit in different threads (and CTAs): scatter the
+        // outputs to their owners' slices, then every CTA resolves its own
+        // range of k, reading Z[L-k] wherever it lives.
+        constexpr int M = L, LQ = TT::LQ;
         const bool full = a.epilogue == EPI_R2C_FULL;
         if constexpr (NST > 1) {
             float2 *region = smem + c * RS;
-            __syncthreads();
+            if constexpr (Q > 1)
+                cg::this_cluster().barrier_wait();
+            else
+                __syncthreads();
 #pragma unroll
-            for (int j = 0; j < NBL; j++)
+            for (int u = 0; u < NBL; u++)
 #pragma unroll
-                for (int m = 0; m < rl; m++)
-                    region[padpos(t + T * (j + m * NBL))] = v[j * rl + m];
-            __syncthreads();
+                for (int m = 0; m < rl; m++) {
+                    const int pos = p0 + TL * u + m * Q * BL;
+                    const int owner = pos / LQ;
+                    float2 *dst = Q > 1 ? cg::this_cluster().map_shared_rank(region, owner) : region;
+                    dst[padpos(pos - owner * LQ)] = v[u * rl + m];
+                }
+            tile_sync<Q>();
             if (valid) {
 #pragma unroll
                 for (int q = 0; q < R; q++) {
-                    const int k = t + T * q;
-                    float2 zk = region[padpos(k)];
+                    const int kl = tl + TL * q;  // local position in this CTA's slice
+                    const int k = j * LQ + kl;
+                    const float2 zk = region[padpos(kl)];
                     if (k == 0) {
                         out[obase] = make_float2(zk.x + zk.y, 0.f);
                         out[obase + (long long)M * a.out_stride] = make_float2(zk.x - zk.y, 0.f);
                     } else {
+                        const int mk = M - k, mo = mk / LQ;
+                        const float2 *src = Q > 1 ? cg::this_cluster().map_shared_rank(region, mo) : region;
                         float2 lo, hi;
-                        r2c_bins(zk, region[padpos(M - k)], __ldg(&a.rtw[k]), lo, hi);
+                        r2c_bins(zk, src[padpos(mk - mo * LQ)], __ldg(&a.rtw[k]), lo, hi);
                         out[obase + (long long)k * a.out_stride] = lo;
                         if (full)
                             out[obase + (long long)(k + M) * a.out_stride] = hi;
                     }
                 }
             }
+            if constexpr (Q > 1)
+                cg::this_cluster().sync();  // slices stay alive until every CTA has read them
         } else {
             // One thread owns the whole transform (L <= 16): natural order in v.
             if (valid) {
@@ -484,40 +572,42 @@ __global__ void __launch_bounds__(C *(L / R)) tile_fft(const TileArgs a)
         return;
     }
 
-    if (!valid)
-        return;
-    const long long ostep = (SMAP == ALONG) ? (long long)T : (long long)T * a.out_stride;
-    float2 *o0 = out + obase + ((SMAP == ALONG) ? (long long)t : (long long)t * a.out_stride);
-    if (a.epilogue == EPI_TWIDDLE) {
+    if (valid) {
+        const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
+        float2 *o0 = out + obase + (long long)p0 * sst;
+        if (a.epilogue == EPI_TWIDDLE) {
 #pragma unroll
-        for (int j = 0; j < NBL; j++)
+            for (int u = 0; u < NBL; u++)
 #pragma unroll
-            for (int m = 0; m < rl; m++) {
-                const int q = j + m * NBL;
-                float2 y = cmul(v[j * rl + m], fourstep_twiddle((unsigned)(t + T * q) * tr, a.tw_scale));
-                if (a.conj & 2)
-                    y.y = -y.y;
-                o0[q * ostep] = y;
-            }
-    } else {
-        const float sg = (a.conj & 2) ? -1.f : 1.f;
+                for (int m = 0; m < rl; m++) {
+                    const int off = TL * u + m * Q * BL;
+                    float2 y = cmul(v[u * rl + m], fourstep_twiddle((unsigned)(p0 + off) * tr, a.tw_scale));
+                    if (a.conj & 2)
+                        y.y = -y.y;
+                    o0[(long long)off * sst] = y;
+                }
+        } else {
+            const float sg = (a.conj & 2) ? -1.f : 1.f;
 #pragma unroll
-        for (int j = 0; j < NBL; j++)
+            for (int u = 0; u < NBL; u++)
 #pragma unroll
-            for (int m = 0; m < rl; m++) {
-                const int q = j + m * NBL;
-                const float2 y = v[j * rl + m];
-                o0[q * ostep] = make_float2(y.x, sg * y.y);
-            }
+                for (int m = 0; m < rl; m++) {
+                    const int off = TL * u + m * Q * BL;
+                    const float2 y = v[u * rl + m];
+                    o0[(long long)off * sst] = make_float2(y.x, sg * y.y);
+                }
+        }
     }
+    if constexpr (Q > 1)
+        cg::this_cluster().barrier_wait();
 }
 
 // Shared memory bytes a tile_fft instantiation needs.
-template <int L, int R, int C, int LMAP, int SMAP>
+template <int L, int R, int C, int Q, int LMAP, int SMAP>
 constexpr size_t tile_smem_bytes()
 {
     return (Sched<L, R>::NST > 1)
-               ? (size_t)C * region_stride<L, C, (LMAP == ACROSS || SMAP == ACROSS)>() * sizeof(float2)
+               ? (size_t)C * region_stride<L / Q, C, (LMAP == ACROSS || SMAP == ACROSS)>() * sizeof(float2)
                : 0;
 }
 

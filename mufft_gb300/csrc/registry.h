@@ -10,21 +10,23 @@ namespace mgb {
 struct TileKernel {
     int L;          // transform length
     int R;          // elements per thread
-    int C;          // transforms per CTA
+    int C;          // transforms per tile
+    int Q;          // CTAs per tile (thread-block cluster size)
     int lmap, smap; // thread maps of the load and store phases
     const void *fn;
-    int threads;
-    size_t smem;
+    int threads;    // per CTA
+    size_t smem;    // per CTA
 };
 
 void register_tiles_along(std::vector<TileKernel> &out);
 void register_tiles_across(std::vector<TileKernel> &out);
 void register_tiles_transpose(std::vector<TileKernel> &out);
 
-// Returns the instantiation for (L, lmap, smap): the one with C transforms
-// per CTA when C > 0, else the preferred one (set_tile_choice) or the first
-// registered.  nullptr if none exists.
-const TileKernel *find_tile(int L, int lmap, int smap, int C = 0, int R = 0);
-bool set_tile_choice(int L, int lmap, int smap, int C, int R = 0);
+// Returns the instantiation for (L, lmap, smap): the one matching the
+// nonzero of C (transforms per tile), R (elements per thread) and Q (cluster
+// size), else the preferred one (set_tile_choice) or the first registered.
+// nullptr if none exists.
+const TileKernel *find_tile(int L, int lmap, int smap, int C = 0, int R = 0, int Q = 0);
+bool set_tile_choice(int L, int lmap, int smap, int C, int R = 0, int Q = 0);
 
 }  // namespace mgb

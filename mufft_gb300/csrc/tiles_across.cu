@@ -5,9 +5,10 @@
 
 namespace mgb {
 
-#define TILE(L, R, C)                                                                              \
-    out.push_back(TileKernel{L, R, C, ACROSS, ACROSS, (const void *)&tile_fft<L, R, C, ACROSS, ACROSS>, \
-                             C *(L / R), tile_smem_bytes<L, R, C, ACROSS, ACROSS>()})
+#define TILE_Q(L, R, C, Q)                                                                            \
+    out.push_back(TileKernel{L, R, C, Q, ACROSS, ACROSS, (const void *)&tile_fft<L, R, C, Q, ACROSS, ACROSS>, \
+                             C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ACROSS, ACROSS>()})
+#define TILE(L, R, C) TILE_Q(L, R, C, 1)
 
 void register_tiles_across(std::vector<TileKernel> &out)
 {
@@ -24,7 +25,8 @@ void register_tiles_across(std::vector<TileKernel> &out)
     TILE(1024, 16, 16);
     TILE(2048, 16, 4);
     TILE(2048, 16, 8);
-    TILE(4096, 16, 4);  // default: measured fastest for the 4096 x 4096 four-step
+    TILE(4096, 16, 4);       // default: measured fastest for the 4096 x 4096 four-step
+    TILE_Q(4096, 16, 4, 4);  // the same tile spread over a 4-CTA cluster
     TILE(4096, 16, 2);
     TILE(4096, 32, 4);
     TILE(4096, 32, 2);

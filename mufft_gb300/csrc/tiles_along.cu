@@ -4,9 +4,10 @@
 
 namespace mgb {
 
-#define TILE(L, R, C)                                                                          \
-    out.push_back(TileKernel{L, R, C, ALONG, ALONG, (const void *)&tile_fft<L, R, C, ALONG, ALONG>, \
-                             C *(L / R), tile_smem_bytes<L, R, C, ALONG, ALONG>()})
+#define TILE_Q(L, R, C, Q)                                                                            \
+    out.push_back(TileKernel{L, R, C, Q, ALONG, ALONG, (const void *)&tile_fft<L, R, C, Q, ALONG, ALONG>, \
+                             C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ALONG, ALONG>()})
+#define TILE(L, R, C) TILE_Q(L, R, C, 1)
 
 void register_tiles_along(std::vector<TileKernel> &out)
 {
@@ -24,8 +25,12 @@ void register_tiles_along(std::vector<TileKernel> &out)
     TILE(4096, 16, 1);
     TILE(8192, 16, 1);
     TILE(8192, 32, 1);
+    TILE_Q(8192, 16, 1, 2);  // clusters: the transform is spread over Q SMs
     TILE(16384, 16, 1);
     TILE(16384, 32, 1);
+    TILE_Q(16384, 16, 1, 4);
+    TILE_Q(32768, 16, 1, 8);
+    TILE_Q(65536, 16, 1, 8);
 }
 
 }  // namespace mgb
