@@ -8,7 +8,7 @@ import numpy as np
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "golden.npz"
 
-# Parity bar of the GPU path against the reference / oracle (the benchmark spec):
+# Parity bar of the GPU path against the reference / oracle:
 # relative L2 error <= 1e-5 for c2c, r2c, c2r and convolution.
 REL_L2_TOL = 1e-5
 
