@@ -71,6 +71,27 @@ int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, cons
 int mufft_gb_execute_plan_1d_launches_async(mufft_plan_1d *plan, void *output, const void *input,
                                             unsigned first, unsigned count, void *stream);
 
+/* ------------------------------------------------- allocation-free execute */
+
+/* No counterpart in the reference.  A forward or inverse c2c transform of N
+ * complex points for callers that must not allocate memory when they
+ * transform -- a real-time audio callback that cannot take cudaMalloc's
+ * latency and implicit synchronisation, or a plugin whose host owns all
+ * device memory.  No plan is needed: the scratch between the two passes of
+ * long transforms and the twiddle table live in fixed device arrays of the
+ * library (2^20 points of scratch, about 8.6 MB per GPU, held until exit).
+ *   N: power of two, 2 <= N <= 2^20 (1048576); larger N returns
+ *      MUFFT_GB_ERR_UNSUPPORTED -- use a plan.
+ *   output, input: device-accessible, N complex each, not overlapping
+ *      (host memory returns MUFFT_GB_ERR_HOST_POINTER).
+ *   stream: cudaStream_t (NULL = legacy default stream); enqueued, not synchronised.
+ * The first call on a device sets up (looks up the arrays' device addresses,
+ * fills the twiddle table, synchronises the device): make it before any
+ * stream capture.  All calls on a device share one scratch array, which keeps
+ * the last call's contents; calls whose kernels overlap on the GPU race on it,
+ * so serialise them (one stream).  Returns MUFFT_GB_OK or an error code. */
+int mufft_gb_execute_c2c_noalloc(unsigned N, int direction, void *output, const void *input, void *stream);
+
 /* ---------------------------------------------------------- introspection */
 
 /* Kernel launches one execute enqueues, and a one-line description of the

@@ -80,6 +80,7 @@ GB_H = [
     ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, C.c_char_p, _sz]),
     ("set_tile_choice", _i, [_u, _i, _i, _u, _u, _u]),
     ("list_tiles", _i, [C.c_char_p, _sz]),
+    ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
     ("device_alloc", _vp, [_sz]),
     ("device_free", None, [_vp]),
     ("memcpy", _i, [_vp, _vp, _sz]),
