@@ -118,6 +118,18 @@ int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned 
  * Affects plans created afterwards. */
 int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_tile,
                              unsigned elems_per_thread, unsigned cluster_ctas);
+/* Passes used for transforms longer than one on-chip tile (16384 points):
+ * 2 (four-step) or 3 (three-level decomposition with smaller tiles); 0
+ * restores the automatic choice.  Affects plans created afterwards. */
+int mufft_gb_set_multipass_levels(unsigned levels);
+/* Inter-pass twiddles of multi-pass transforms from a per-plan FP64 table
+ * (1) or from sincospif (0); -1 restores the automatic choice by tile length.
+ * Affects plans created afterwards. */
+int mufft_gb_set_twiddle_table(int mode);
+/* Three-level transforms of N1 x 65536 points run their last two passes as one
+ * persistent launch whose intermediate stays in L2 (enable = 1) or as two
+ * launches (0, default).  Affects plans created afterwards. */
+int mufft_gb_set_fused_passes(int enable);
 /* Writes "L=.. R=.. C=.. Q=.. along/across threads=.. smem=..; ..." for every
  * compiled tile kernel; returns the full length. */
 int mufft_gb_list_tiles(char *buf, size_t size);

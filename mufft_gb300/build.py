@@ -47,7 +47,7 @@ def _compile(src: Path, verbose: bool) -> tuple[Path, str]:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stdout}\n{res.stderr}")
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stdout}\n{res.stderr[:4000]}")
     return obj, res.stderr
 
 

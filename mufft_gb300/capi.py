@@ -79,6 +79,9 @@ GB_H = [
     ("plan_2d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, C.c_char_p, _sz]),
     ("set_tile_choice", _i, [_u, _i, _i, _u, _u, _u]),
+    ("set_multipass_levels", _i, [_u]),
+    ("set_twiddle_table", _i, [_i]),
+    ("set_fused_passes", _i, [_i]),
     ("list_tiles", _i, [C.c_char_p, _sz]),
     ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
     ("device_alloc", _vp, [_sz]),

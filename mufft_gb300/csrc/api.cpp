@@ -20,12 +20,14 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/fft.h"
 #include "../../include/mufft_gb300.h"
+#include "bc_fused.h"
 #include "common.h"
 #include "misc_kernels.h"
 #include "registry.h"
@@ -254,7 +256,7 @@ bool is_device_accessible(const void *p)
 // ================================================================ passes
 
 enum Role { ROLE_NONE = 0, ROLE_IN, ROLE_OUT, ROLE_IN2, ROLE_SCRATCH };
-enum PassType { PASS_TILE = 0, PASS_R2C_FIXUP = 1 };
+enum PassType { PASS_TILE = 0, PASS_R2C_FIXUP = 1, PASS_BC = 2 };
 
 struct Pass {
     PassType type = PASS_TILE;
@@ -266,6 +268,10 @@ struct Pass {
     long long M = 0, dist = 0;
     unsigned batch = 1;
     int full = 0;
+    // fused B/C passes (bc_fused.cu): y is the scratch, x the role out_role
+    BcArgs bc{};
+    size_t bc_counter_bytes = 0;
+    unsigned bc_grid = 0;
 };
 
 struct Buffers {
@@ -299,6 +305,7 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             a.out = (float2 *)pick(p.out_role, b);
             a.in2 = (const float2 *)pick(p.in2_role, b);
             void *args[] = {&a};
+            const size_t smem = a.tw_lo ? p.k->smem : p.k->smem_ex;
             cudaError_t e;
             if (p.k->Q > 1) {
                 // one tile per cluster of Q CTAs (distributed shared memory)
@@ -306,7 +313,7 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                 cudaLaunchAttribute attr[1];
                 cfg.gridDim = dim3(p.grid.x * p.k->Q, p.grid.y, p.grid.z);
                 cfg.blockDim = dim3(p.k->threads);
-                cfg.dynamicSmemBytes = p.k->smem;
+                cfg.dynamicSmemBytes = smem;
                 cfg.stream = st;
                 attr[0].id = cudaLaunchAttributeClusterDimension;
                 attr[0].val.clusterDim.x = p.k->Q;
@@ -316,8 +323,19 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                 cfg.numAttrs = 1;
                 e = cudaLaunchKernelExC(&cfg, p.k->fn, args);
             } else {
-                e = cudaLaunchKernel(p.k->fn, p.grid, dim3(p.k->threads), args, p.k->smem, st);
+                e = cudaLaunchKernel(p.k->fn, p.grid, dim3(p.k->threads), args, smem, st);
             }
+            if (e != cudaSuccess)
+                return e;
+        } else if (p.type == PASS_BC) {
+            BcArgs a = p.bc;
+            a.y = (const float2 *)b.scratch;
+            a.x = (float2 *)pick(p.out_role, b);
+            cudaError_t e = cudaMemsetAsync(a.counters, 0, p.bc_counter_bytes, st);
+            if (e != cudaSuccess)
+                return e;
+            void *args[] = {&a};
+            e = cudaLaunchKernel(bc_kernel(), dim3(p.bc_grid), dim3(bc_threads()), args, bc_smem_bytes(), st);
             if (e != cudaSuccess)
                 return e;
         } else {
@@ -352,6 +370,9 @@ std::string describe(const std::vector<Pass> &ps)
                      i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue), p.a.conj);
+        else if (p.type == PASS_BC)
+            snprintf(buf, sizeof(buf), "%sfused_bc 256x256 rows=%u blocks=%u ring=%u grid=%u", i ? "; " : "",
+                     p.bc.n1, p.bc.nblk, p.bc.ring_slots, p.bc_grid);
         else
             snprintf(buf, sizeof(buf), "%sr2c_fixup M=%lld batch=%u full=%d", i ? "; " : "", p.M, p.batch, p.full);
         s += buf;
@@ -375,15 +396,80 @@ struct FftSpec {
 // Device tables and scratch a schedule needs; allocated unless `dry`.
 struct PlanResources {
     float2 *rtw = nullptr;
+    float2 *twlo = nullptr;   // multi-pass: W_M^(k*c) of the first column pass
+    float2 *twlo2 = nullptr;  // three-level: the same for the second column pass
     float2 *scratch = nullptr;
     size_t scratch_bytes = 0;
+    float2 *ring = nullptr;       // fused B/C: L2-resident ring of row blocks
+    unsigned *counters = nullptr; // fused B/C: task counters
+    int *err = nullptr;           // device error flag of bounded waits
     void release()
     {
         cudaFree(rtw);
+        cudaFree(twlo);
+        cudaFree(twlo2);
         cudaFree(scratch);
-        rtw = scratch = nullptr;
+        cudaFree(ring);
+        cudaFree(counters);
+        cudaFree(err);
+        rtw = twlo = twlo2 = scratch = ring = nullptr;
+        counters = nullptr;
+        err = nullptr;
     }
 };
+
+// Multi-pass depth for transforms longer than one tile: 0 = automatic
+// (set with mufft_gb_set_multipass_levels).
+std::atomic<int> g_levels{0};
+// Four-step twiddles of column passes from the per-plan table (1), from
+// sincospif (0), or by tile length (-1: table for L <= 512, where the extra
+// shared memory costs no occupancy; longer tiles are bound by load/store
+// issue, which sincospif on the otherwise idle XU pipe avoids).
+std::atomic<int> g_twiddle_table{-1};
+// Fuse the last two passes of M = N1 x 65536 transforms into one persistent
+// launch with an L2-resident intermediate (1), or run them separately (0,
+// default: the separate passes measured faster on GB300 -- they are bound by
+// instruction issue and latency, not by the HBM traffic the fusion saves).
+std::atomic<int> g_fused_bc{0};
+
+bool use_twiddle_table(const TileKernel *k)
+{
+    const int t = g_twiddle_table.load();
+    return k->has_thi && (t == 1 || (t < 0 && k->L <= 512));
+}
+
+// W_M^(k*c) for k < L, c < C: the per-column half of a four-step twiddle.
+bool upload_twlo(unsigned L, int C, unsigned long long M, float2 *&dst)
+{
+    std::vector<float2> lo((size_t)L * C);
+    for (unsigned k = 0; k < L; k++)
+        for (int c = 0; c < C; c++) {
+            double ph = -2.0 * M_PI * (double)((unsigned long long)k * c % M) / (double)M;
+            lo[(size_t)k * C + c] = make_float2((float)std::cos(ph), (float)std::sin(ph));
+        }
+    dst = upload(lo);
+    return dst != nullptr;
+}
+
+// Column pass of a multi-pass transform: `ncols` columns of length L (stride
+// `stride`), output twiddled by W_Mtw^(k*column).
+Pass column_pass(const TileKernel *k, const float2 *tw, unsigned L, unsigned ncols, long long stride,
+                 unsigned long long Mtw, const float2 *twlo)
+{
+    Pass p;
+    p.k = k;
+    p.a.in_stride = p.a.out_stride = stride;
+    p.a.in_dist = p.a.out_dist = 1;
+    p.a.ntrans = ncols;
+    p.a.epilogue = EPI_TWIDDLE;
+    p.a.tw = tw;
+    p.a.tw_scale = 2.0f / (float)Mtw;
+    p.a.tw_mask = (unsigned)(Mtw - 1);
+    p.a.tw_lo = use_twiddle_table(k) ? twlo : nullptr;
+    p.a.scale = 1.0f;
+    (void)L;
+    return p;
+}
 
 bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bool dry,
                       std::vector<Pass> &out)
@@ -420,8 +506,200 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
         return true;
     }
 
-    // Four-step: M = N1 * N2, x[n1*N2 + n2], X[k1 + N1*k2].
     const unsigned lg = ilog2u(M);
+    int levels = g_levels.load();
+    if (levels == 0)
+        levels = lg >= 22 ? 3 : 2;  // measured crossover on GB300
+    if (levels == 3 && lg >= 20 && g_fused_bc.load()) {
+        // M = N1 x 65536: pass A column tiles of length N1, then the fused
+        // persistent B/C launch with an L2-resident intermediate.
+        const unsigned N1 = M >> 16;
+        const TileKernel *ka = find_tile((int)N1, ACROSS, ACROSS);
+        if (ka && N1 % 16 == 0 && s.batch <= 65535) {
+            const unsigned long long MR = 65536;
+            const unsigned blk_per_item = N1 / 16;
+            const unsigned nblk = blk_per_item * s.batch;
+            const unsigned ring = nblk < 2 ? 1 : (nblk < 4 ? 2 : 4);
+            Pass pbc;
+            pbc.type = PASS_BC;
+            pbc.out_role = s.out_role;
+            pbc.bc.n1 = N1;
+            pbc.bc.nblk = nblk;
+            pbc.bc.blk_per_item = blk_per_item;
+            pbc.bc.ring_slots = ring;
+            pbc.bc.y_item = M;
+            pbc.bc.x_item = s.out_dist;
+            pbc.bc_counter_bytes = (2 * (size_t)nblk + 1) * sizeof(unsigned);
+            const TileKernel *kb = find_tile(256, ACROSS, ACROSS, 16, 16, 1);
+            float2 *twlo_b = nullptr;
+            if (!dry) {
+                res.scratch_bytes = (size_t)M * s.batch * sizeof(float2);
+                if (!cuda_ok(cudaMalloc(&res.scratch, res.scratch_bytes), "cudaMalloc(scratch)") ||
+                    !cuda_ok(cudaMalloc(&res.ring, (size_t)ring * 16 * MR * sizeof(float2)), "cudaMalloc(ring)") ||
+                    !cuda_ok(cudaMalloc(&res.counters, pbc.bc_counter_bytes), "cudaMalloc(counters)") ||
+                    !cuda_ok(cudaMalloc(&res.err, sizeof(int)), "cudaMalloc(err)") ||
+                    !cuda_ok(cudaMemset(res.err, 0, sizeof(int)), "cudaMemset(err)"))
+                    return false;
+                if ((use_twiddle_table(ka) && !upload_twlo(N1, ka->C, M, res.twlo)) ||
+                    !upload_twlo(256, 16, MR, res.twlo2))
+                    return false;
+                twlo_b = res.twlo2;
+                int dev = 0, sms = 0, per_sm = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bc_kernel(), bc_threads(),
+                                                                           bc_smem_bytes()),
+                             "occupancy"))
+                    return false;
+                pbc.bc_grid = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
+            } else {
+                pbc.bc_grid = 0;
+            }
+            pbc.bc.ring = res.ring;
+            pbc.bc.counters = res.counters;
+            pbc.bc.err = res.err;
+            // pass-B template: 256-point columns over stride 256 in one row, W_65536 twiddle
+            TileArgs &tb = pbc.bc.b;
+            tb.in_stride = tb.out_stride = 256;
+            tb.in_dist = tb.out_dist = 1;
+            tb.ntrans = 256;
+            tb.epilogue = EPI_TWIDDLE;
+            tb.tw = tw;
+            tb.tw_scale = 2.0f / 65536.0f;
+            tb.tw_mask = 65535u;
+            tb.tw_lo = (kb && kb->has_thi) ? twlo_b : nullptr;
+            tb.scale = 1.0f;
+            // pass-C template: 16 rows of 256 contiguous points, stores across rows
+            TileArgs &tc = pbc.bc.c;
+            tc.in_stride = 1;
+            tc.in_dist = (long long)MR;
+            tc.out_stride = (long long)N1 * 256;
+            tc.out_dist = 1;
+            tc.ntrans = 16;
+            tc.conj = s.conj_out ? 2 : 0;
+            tc.tw = tw;
+            tc.scale = 1.0f;
+
+            Pass pa = column_pass(ka, tw, N1, (unsigned)MR, (long long)MR, M, res.twlo);
+            pa.a.in_batch = s.in_dist;
+            pa.a.out_batch = M;
+            pa.a.conj = s.conj_in ? 1 : 0;
+            pa.a.prologue = s.prologue;
+            pa.a.half = s.half;
+            pa.a.rtw = res.rtw;
+            pa.a.mirror_len = M;
+            pa.a.mirror_ldist = 1;
+            pa.a.scale = s.scale;
+            pa.in_role = s.in_role;
+            pa.in2_role = s.in2_role;
+            pa.out_role = ROLE_SCRATCH;
+            pa.grid = dim3((unsigned)((MR + ka->C - 1) / ka->C), s.batch);
+            out.push_back(pa);
+            out.push_back(pbc);
+            if (r2c) {
+                Pass p3;
+                p3.type = PASS_R2C_FIXUP;
+                p3.a.rtw = res.rtw;
+                p3.out_role = s.out_role;
+                p3.M = M;
+                p3.dist = s.out_dist;
+                p3.batch = s.batch;
+                p3.full = s.epilogue == EPI_R2C_FULL;
+                out.push_back(p3);
+            }
+            return true;
+        }
+    }
+    if (levels == 3 && lg >= 12) {
+        // Three levels, M = N1 * N2 * N3 (near-equal powers of two, each tile
+        // small enough for several CTAs per SM):
+        //   A: columns of length N1 over m < N2*N3 (stride N2*N3), twiddle W_M^(k1*m)
+        //   B: in place, per row k1: columns of length N2 over n3 < N3, twiddle
+        //      W_(N2*N3)^(k2*n3)
+        //   C: rows (k1, k2) of length N3, stores transposed to X[k1 + N1*(k2 + N2*k3)]
+        const unsigned l1 = lg / 3, l2 = (lg - l1) / 2, l3 = lg - l1 - l2;
+        const unsigned N1 = 1u << l1, N2 = 1u << l2, N3 = 1u << l3;
+        const unsigned long long MR = (unsigned long long)N2 * N3;
+        if (s.batch > 65535u / N2 || s.batch > 65535) {
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "batch %u too large for three-level lengths", s.batch);
+            return false;
+        }
+        const TileKernel *ka = find_tile((int)N1, ACROSS, ACROSS);
+        const TileKernel *kb = find_tile((int)N2, ACROSS, ACROSS);
+        const TileKernel *kr = find_tile((int)N3, ALONG, ACROSS);
+        if (!ka || !kb || !kr) {
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "no three-level kernels for %u x %u x %u", N1, N2, N3);
+            return false;
+        }
+        float2 *twlo_b = nullptr;
+        if (!dry) {
+            res.scratch_bytes = (size_t)M * s.batch * sizeof(float2);
+            if (!cuda_ok(cudaMalloc(&res.scratch, res.scratch_bytes), "cudaMalloc(scratch)"))
+                return false;
+            if ((use_twiddle_table(ka) && !upload_twlo(N1, ka->C, M, res.twlo)) ||
+                (use_twiddle_table(kb) && !upload_twlo(N2, kb->C, MR, res.twlo2)))
+                return false;
+            twlo_b = res.twlo2;
+        }
+        Pass pa = column_pass(ka, tw, N1, (unsigned)MR, (long long)MR, M, res.twlo);
+        pa.a.in_batch = s.in_dist;
+        pa.a.out_batch = M;
+        pa.a.conj = s.conj_in ? 1 : 0;
+        pa.a.prologue = s.prologue;
+        pa.a.half = s.half;
+        pa.a.rtw = res.rtw;
+        pa.a.mirror_len = M;
+        pa.a.mirror_ldist = 1;
+        pa.a.scale = s.scale;
+        pa.in_role = s.in_role;
+        pa.in2_role = s.in2_role;
+        pa.out_role = ROLE_SCRATCH;
+        pa.grid = dim3((unsigned)((MR + ka->C - 1) / ka->C), s.batch);
+        out.push_back(pa);
+
+        Pass pb = column_pass(kb, tw, N2, N3, (long long)N3, MR, twlo_b);
+        pb.a.ysplit = N1;
+        pb.a.in_batch = pb.a.out_batch = (long long)MR;
+        pb.a.in_batch2 = pb.a.out_batch2 = M;
+        pb.in_role = ROLE_SCRATCH;
+        pb.out_role = ROLE_SCRATCH;
+        pb.grid = dim3((N3 + kb->C - 1) / kb->C, N1 * s.batch);
+        out.push_back(pb);
+
+        Pass pc;
+        pc.k = kr;
+        pc.a.in_stride = 1;
+        pc.a.in_dist = (long long)MR;
+        pc.a.out_stride = (long long)N1 * N2;
+        pc.a.out_dist = 1;
+        pc.a.ysplit = N2;
+        pc.a.in_batch = N3;
+        pc.a.out_batch = N1;
+        pc.a.in_batch2 = M;
+        pc.a.out_batch2 = s.out_dist;
+        pc.a.ntrans = N1;
+        pc.a.conj = s.conj_out ? 2 : 0;
+        pc.a.tw = tw;
+        pc.a.scale = 1.0f;
+        pc.in_role = ROLE_SCRATCH;
+        pc.out_role = s.out_role;
+        pc.grid = dim3((N1 + kr->C - 1) / kr->C, N2 * s.batch);
+        out.push_back(pc);
+        if (r2c) {
+            Pass p3;
+            p3.type = PASS_R2C_FIXUP;
+            p3.a.rtw = res.rtw;
+            p3.out_role = s.out_role;
+            p3.M = M;
+            p3.dist = s.out_dist;
+            p3.batch = s.batch;
+            p3.full = s.epilogue == EPI_R2C_FULL;
+            out.push_back(p3);
+        }
+        return true;
+    }
+
+    // Four-step: M = N1 * N2, x[n1*N2 + n2], X[k1 + N1*k2].
     const unsigned N1 = 1u << (lg / 2), N2 = M / N1;
     if (N2 > kMaxTile) {
         set_error(MUFFT_GB_ERR_UNSUPPORTED, "transform length %u exceeds the two-pass limit", M);
@@ -440,6 +718,8 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     if (!dry) {
         res.scratch_bytes = (size_t)M * s.batch * sizeof(float2);
         if (!cuda_ok(cudaMalloc(&res.scratch, res.scratch_bytes), "cudaMalloc(scratch)"))
+            return false;
+        if (use_twiddle_table(kc) && !upload_twlo(N1, kc->C, M, res.twlo))
             return false;
     }
     Pass p1;
@@ -461,6 +741,8 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p1.a.mirror_ldist = 1;
     p1.a.scale = s.scale;
     p1.a.tw_scale = 2.0f / (float)M;
+    p1.a.tw_mask = M - 1;
+    p1.a.tw_lo = use_twiddle_table(kc) ? res.twlo : nullptr;
     p1.in_role = s.in_role;
     p1.in2_role = s.in2_role;
     p1.out_role = ROLE_SCRATCH;
@@ -733,6 +1015,14 @@ int exec_1d(mufft_plan_1d *pl, void *out, const void *in, const void *in2, cudaS
         return t_err;
     if (sync && !cuda_ok(cudaStreamSynchronize(st), "execute"))
         return t_err;
+    if (sync && pl->res.err) {
+        int e = 0;
+        if (cuda_ok(cudaMemcpy(&e, pl->res.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag") && e) {
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "a bounded wait in the fused passes timed out");
+            cudaMemset(pl->res.err, 0, sizeof(int));
+            return t_err;
+        }
+    }
     return MUFFT_GB_OK;
 }
 
@@ -1292,6 +1582,32 @@ int mufft_gb_device_synchronize(void)
 }
 
 // ========================================================= tile choice
+
+int mufft_gb_set_twiddle_table(int mode)
+{
+    if (mode < -1 || mode > 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "mode must be -1 (automatic), 0 or 1");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_twiddle_table.store(mode);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_fused_passes(int enable)
+{
+    g_fused_bc.store(enable ? 1 : 0);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_multipass_levels(unsigned levels)
+{
+    if (levels != 0 && levels != 2 && levels != 3) {
+        set_error(MUFFT_GB_ERR_INVALID, "levels must be 0 (automatic), 2 or 3");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_levels.store((int)levels);
+    return MUFFT_GB_OK;
+}
 
 int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_tile,
                              unsigned elems_per_thread, unsigned cluster_ctas)

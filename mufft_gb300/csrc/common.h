@@ -60,6 +60,10 @@ struct TileArgs {
     float2 *out;
     long long in_stride, in_dist, in_batch;
     long long out_stride, out_dist, out_batch;
+    // two-level batch: blockIdx.y = g + ysplit*b advances g*in_batch + b*in_batch2
+    // (ysplit 0: one level, blockIdx.y*in_batch)
+    unsigned ysplit;
+    long long in_batch2, out_batch2;
     unsigned ntrans;
     int conj;                 // 1: inverse transform by conjugating in and out
     int prologue;
@@ -73,8 +77,12 @@ struct TileArgs {
     // convolution prologues
     const float2 *in2;        // second spectrum (B)
     float scale;
-    // four-step twiddle W_N^m = exp(-2*pi*i*m/N): tw_scale = 2/N
+    // four-step twiddle W_N^m = exp(-2*pi*i*m/N): tw_scale = 2/N, tw_mask = N - 1;
+    // for column tiles of C transforms tw_lo[k*C + c] = W_N^(k*c) (or null:
+    // then every twiddle comes from sincospif)
     float tw_scale;
+    unsigned tw_mask;
+    const float2 *tw_lo;
 };
 
 }  // namespace mgb

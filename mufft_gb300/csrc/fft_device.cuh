@@ -347,7 +347,18 @@ __device__ __forceinline__ float2 c2r_fixup(float2 a, float2 bm, float2 w)
 // Stage-0 load: register u*r + m <- element p = j*B + tl + TL*u + m*Q*B of
 // transform `tr`.  ALONG loads have unit stride (the planner only builds them
 // that way), so addresses are a base plus constant offsets.
-template <int L, int R, int Q, int LMAP>
+// Global loads: read-only path, or (COH) L2-coherent loads for data written
+// earlier in the same launch by other CTAs.
+template <bool COH>
+__device__ __forceinline__ float2 gload(const float2 *p)
+{
+    if constexpr (COH)
+        return __ldcg(p);
+    else
+        return __ldg(p);
+}
+
+template <int L, int R, int Q, int LMAP, bool COH = false>
 __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__restrict__ in,
                                             const float2 *__restrict__ in2, unsigned tr, int j, int tl,
                                             float2 (&v)[R])
@@ -372,7 +383,7 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
 #pragma unroll
             for (int m = 0; m < r; m++)
                 if (m < mlim)
-                    v[u * r + m] = __ldg(f + (long long)(TL * u + m * Q * B) * sst);
+                    v[u * r + m] = gload<COH>(f + (long long)(TL * u + m * Q * B) * sst);
         break;
     }
     case PRO_MUL: {
@@ -383,7 +394,7 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
             for (int m = 0; m < r; m++)
                 if (m < mlim) {
                     const long long o = (long long)(TL * u + m * Q * B) * sst;
-                    v[u * r + m] = cscale(cmul(__ldg(f + o), __ldg(g + o)), a.scale);
+                    v[u * r + m] = cscale(cmul(gload<COH>(f + o), gload<COH>(g + o)), a.scale);
                 }
         break;
     }
@@ -399,10 +410,10 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
                 if (m < mlim) {
                     const long long local = lfirst + (long long)(TL * u + m * Q * B) * a.in_stride;
                     const long long ia = tb + local, ib = tb + a.mirror_len - local;
-                    float2 xa = __ldg(&in[ia]), xb = __ldg(&in[ib]);
+                    float2 xa = gload<COH>(&in[ia]), xb = gload<COH>(&in[ib]);
                     if (mul) {
-                        xa = cscale(cmul(xa, __ldg(&in2[ia])), a.scale);
-                        xb = cscale(cmul(xb, __ldg(&in2[ib])), a.scale);
+                        xa = cscale(cmul(xa, gload<COH>(&in2[ia])), a.scale);
+                        xb = cscale(cmul(xb, gload<COH>(&in2[ib])), a.scale);
                     }
                     v[u * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
                 }
@@ -416,11 +427,13 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
     }
 }
 
-// W_N^m = exp(-2*pi*i*m/N) for m < N <= 2^28, scale = 2/N.  sincospif gets
-// an exactly representable argument: m itself when m < 2^24, otherwise the
-// product of the twiddles of m's high and low 12-bit parts.
-__device__ __forceinline__ float2 fourstep_twiddle(unsigned m, float scale)
+// W_N^m = exp(-2*pi*i*m/N) for N <= 2^28 a power of two, scale = 2/N; m is
+// reduced mod N.  sincospif gets an exactly representable argument: m itself
+// when m < 2^24, otherwise the product of the twiddles of m's high and low
+// 12-bit parts.
+__device__ __forceinline__ float2 fourstep_twiddle(unsigned m, float scale, unsigned mask)
 {
+    m &= mask;
     float s, c;
     if (m < (1u << 24)) {
         sincospif((float)m * scale, &s, &c);
@@ -441,6 +454,34 @@ __device__ __forceinline__ void r2c_bins(float2 zk, float2 zmk, float2 w, float2
     lo = cscale(cadd(fe, fo), 0.5f);
     hi = cscale(csub(fe, fo), 0.5f);
 }
+
+// Shared memory of a tile: the exchange slices ...
+template <int L, int R, int C, int Q, int LMAP, int SMAP>
+__host__ __device__ constexpr size_t tile_exchange_bytes()
+{
+    return (Sched<L, R>::NST > 1)
+               ? (size_t)C * region_stride<L / Q, C, (LMAP == ACROSS || SMAP == ACROSS)>() * sizeof(float2)
+               : 0;
+}
+
+constexpr size_t kMaxSmemPerCta = 227 * 1024;
+
+// ... and, for single-CTA column passes where it fits, the per-tile half of
+// the four-step twiddle (L values); without it the twiddles come from sincospif.
+template <int L, int R, int C, int Q, int LMAP, int SMAP>
+__host__ __device__ constexpr bool tile_has_thi()
+{
+    return Q == 1 && LMAP == ACROSS && SMAP == ACROSS &&
+           tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() + (size_t)L * sizeof(float2) <= kMaxSmemPerCta;
+}
+
+template <int L, int R, int C, int Q, int LMAP, int SMAP>
+__host__ __device__ constexpr size_t tile_smem_bytes()
+{
+    return tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() +
+           (tile_has_thi<L, R, C, Q, LMAP, SMAP>() ? (size_t)L * sizeof(float2) : 0);
+}
+
 
 // --------------------------------------------------------------- kernel
 
@@ -465,14 +506,19 @@ __device__ __forceinline__ void run_stages(float2 (&v)[R], int j, int &c, int &t
 
 // Threads of one CTA, and the CTAs per SM the register budget is sized for:
 // 16-element tiles are held to 64 registers so that 2048 threads fit.
-template <int L, int R, int C, int Q> constexpr int tile_threads() { return C * (L / (R * Q)); }
-template <int L, int R, int C, int Q> constexpr int tile_min_blocks()
+template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_threads() { return C * (L / (R * Q)); }
+template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min_blocks()
 {
     return R <= 16 ? (tile_threads<L, R, C, Q>() >= 1024 ? 1 : 1024 / tile_threads<L, R, C, Q>()) : 1;
 }
 
-template <int L, int R, int C, int Q, int LMAP, int SMAP>
-__global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L, R, C, Q>()) tile_fft(const TileArgs a)
+// One tile of C transforms: load, all stages, store.  `tile` selects the
+// transforms tile*C .. tile*C + C - 1; ioff / ooff shift the input / output
+// base (batches); j is the CTA's rank in its cluster.  COH: load with
+// L2-coherent loads (input written earlier in the same launch).
+template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH>
+__device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
+                                          float2 *smem)
 {
     using S = Sched<L, R>;
     using TT = Tile<L, R, Q>;
@@ -480,23 +526,29 @@ __global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L,
     constexpr int RS = region_stride<TT::LQ, C, (LMAP == ACROSS || SMAP == ACROSS)>();
     static_assert(NST > 1 || LMAP == SMAP, "single-stage tiles cannot change the thread map");
     static_assert(NST > 1 || Q == 1, "single-stage tiles are not split over a cluster");
-    extern __shared__ float2 smem[];
 
-    const float2 *in = a.in + (long long)blockIdx.y * a.in_batch;
-    const float2 *in2 = a.in2 ? a.in2 + (long long)blockIdx.y * a.in_batch : nullptr;
-    float2 *out = a.out + (long long)blockIdx.y * a.out_batch;
-    int j = 0;
-    unsigned tile = blockIdx.x;
-    if constexpr (Q > 1) {
-        j = (int)cg::this_cluster().block_rank();
-        tile = blockIdx.x / Q;
-    }
+    const float2 *in = a.in + ioff;
+    const float2 *in2 = a.in2 ? a.in2 + ioff : nullptr;
+    float2 *out = a.out + ooff;
     const unsigned tile0 = tile * C;
+
+    static_assert(tile_smem_bytes<L, R, C, Q, LMAP, SMAP>() <= kMaxSmemPerCta, "tile exceeds shared memory");
+    if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
+        // Four-step twiddle, per-tile half: W_N^(k*C*tile) for every output k
+        // (the per-column half W_N^(k*c) comes from the plan's table tw_lo).
+        if (a.epilogue == EPI_TWIDDLE && a.tw_lo) {
+            float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
+            for (int k = threadIdx.x; k < L; k += tile_threads<L, R, C, Q>())
+                thi[k] = fourstep_twiddle((unsigned)k * (unsigned)(C * tile), a.tw_scale, a.tw_mask);
+            if constexpr (NST == 1)
+                __syncthreads();
+        }
+    }
 
     float2 v[R];
     int c, tl;
     split_tid<LMAP, C, TL>(threadIdx.x, c, tl);
-    load_stage0<L, R, Q, LMAP>(a, in, in2, tile0 + c, j, tl, v);
+    load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
     stage_compute<L, R, Q, 0>(v, j, tl, a.tw);
     run_stages<L, R, C, Q, LMAP, SMAP, 1>(v, j, c, tl, smem, a.tw);
     // No CTA of the cluster may leave while others still read its slice.
@@ -576,12 +628,25 @@ __global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L,
         const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
         float2 *o0 = out + obase + (long long)p0 * sst;
         if (a.epilogue == EPI_TWIDDLE) {
+            // W_N^(k*n) for output k of column n = tile*C + c.
+            // W_N^(k*C*tile), filled at kernel start, after the exchange slices
+            float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
 #pragma unroll
             for (int u = 0; u < NBL; u++)
 #pragma unroll
                 for (int m = 0; m < rl; m++) {
                     const int off = TL * u + m * Q * BL;
-                    float2 y = cmul(v[u * rl + m], fourstep_twiddle((unsigned)(p0 + off) * tr, a.tw_scale));
+                    const int k = p0 + off;
+                    float2 w;
+                    if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
+                        if (a.tw_lo)
+                            w = cmul(__ldg(&a.tw_lo[k * C + c]), thi[k]);
+                        else
+                            w = fourstep_twiddle((unsigned)k * tr, a.tw_scale, a.tw_mask);
+                    } else {
+                        w = fourstep_twiddle((unsigned)k * tr, a.tw_scale, a.tw_mask);
+                    }
+                    float2 y = cmul(v[u * rl + m], w);
                     if (a.conj & 2)
                         y.y = -y.y;
                     o0[(long long)off * sst] = y;
@@ -602,13 +667,26 @@ __global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L,
         cg::this_cluster().barrier_wait();
 }
 
-// Shared memory bytes a tile_fft instantiation needs.
 template <int L, int R, int C, int Q, int LMAP, int SMAP>
-constexpr size_t tile_smem_bytes()
+__global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L, R, C, Q>()) tile_fft(const TileArgs a)
 {
-    return (Sched<L, R>::NST > 1)
-               ? (size_t)C * region_stride<L / Q, C, (LMAP == ACROSS || SMAP == ACROSS)>() * sizeof(float2)
-               : 0;
+    extern __shared__ float2 smem[];
+    long long ioff, ooff;
+    if (a.ysplit) {
+        const unsigned g = blockIdx.y % a.ysplit, b = blockIdx.y / a.ysplit;
+        ioff = (long long)g * a.in_batch + (long long)b * a.in_batch2;
+        ooff = (long long)g * a.out_batch + (long long)b * a.out_batch2;
+    } else {
+        ioff = (long long)blockIdx.y * a.in_batch;
+        ooff = (long long)blockIdx.y * a.out_batch;
+    }
+    int j = 0;
+    unsigned tile = blockIdx.x;
+    if constexpr (Q > 1) {
+        j = (int)cg::this_cluster().block_rank();
+        tile = blockIdx.x / Q;
+    }
+    tile_body<L, R, C, Q, LMAP, SMAP, false>(a, tile, j, ioff, ooff, smem);
 }
 
 }  // namespace mgb

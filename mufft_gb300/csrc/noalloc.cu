@@ -122,7 +122,8 @@ int set_up(int dev)
 cudaError_t launch(const TileKernel *k, TileArgs &a, unsigned ntrans, cudaStream_t st)
 {
     void *args[] = {&a};
-    return cudaLaunchKernel(k->fn, dim3((ntrans + k->C - 1) / k->C), dim3(k->threads), args, k->smem, st);
+    return cudaLaunchKernel(k->fn, dim3((ntrans + k->C - 1) / k->C), dim3(k->threads), args,
+                            a.tw_lo ? k->smem : k->smem_ex, st);
 }
 
 bool device_pointer(const void *p)
@@ -194,6 +195,7 @@ extern "C" int mufft_gb_execute_c2c_noalloc(unsigned N, int direction, void *out
     a.conj = inv ? 1 : 0;
     a.epilogue = EPI_TWIDDLE;
     a.tw_scale = 2.0f / (float)N;
+    a.tw_mask = N - 1;
     e = launch(d.cols[lg], a, N2, st);
     if (e != cudaSuccess)
         return (int)e;

@@ -16,6 +16,8 @@ struct TileKernel {
     const void *fn;
     int threads;    // per CTA
     size_t smem;    // per CTA
+    bool has_thi;   // column pass that takes the four-step twiddle table tw_lo
+    size_t smem_ex; // per CTA without the four-step table region (launches with tw_lo == null)
 };
 
 void register_tiles_along(std::vector<TileKernel> &out);

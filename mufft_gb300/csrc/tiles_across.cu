@@ -7,7 +7,8 @@ namespace mgb {
 
 #define TILE_Q(L, R, C, Q)                                                                            \
     out.push_back(TileKernel{L, R, C, Q, ACROSS, ACROSS, (const void *)&tile_fft<L, R, C, Q, ACROSS, ACROSS>, \
-                             C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ACROSS, ACROSS>()})
+                             C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ACROSS, ACROSS>(),                \
+                             tile_has_thi<L, R, C, Q, ACROSS, ACROSS>(), tile_exchange_bytes<L, R, C, Q, ACROSS, ACROSS>()})
 #define TILE(L, R, C) TILE_Q(L, R, C, 1)
 
 void register_tiles_across(std::vector<TileKernel> &out)

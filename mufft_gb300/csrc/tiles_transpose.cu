@@ -7,7 +7,8 @@ namespace mgb {
 
 #define TILE_Q(L, R, C, Q)                                                                            \
     out.push_back(TileKernel{L, R, C, Q, ALONG, ACROSS, (const void *)&tile_fft<L, R, C, Q, ALONG, ACROSS>, \
-                             C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ALONG, ACROSS>()})
+                             C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ALONG, ACROSS>(),                \
+                             tile_has_thi<L, R, C, Q, ALONG, ACROSS>(), tile_exchange_bytes<L, R, C, Q, ALONG, ACROSS>()})
 #define TILE(L, R, C) TILE_Q(L, R, C, 1)
 
 void register_tiles_transpose(std::vector<TileKernel> &out)

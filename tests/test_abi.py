@@ -126,11 +126,28 @@ def test_single_pass_schedule(lib):
     assert "pro=c2r" in s
 
 
-def test_four_step_schedule(lib):
-    s = _sched(lib, 1 << 24, 0)
-    parts = s.split("; ")
-    assert len(parts) == 2
-    assert "L=4096" in parts[0] and "across/across" in parts[0] and "epi=twiddle" in parts[0]
-    assert "L=4096" in parts[1] and "along/across" in parts[1]
+def test_multipass_schedules(lib):
+    try:
+        assert lib.gb_set_multipass_levels(2) == 0
+        parts = _sched(lib, 1 << 24, 0).split("; ")
+        assert len(parts) == 2
+        assert "L=4096" in parts[0] and "across/across" in parts[0] and "epi=twiddle" in parts[0]
+        assert "L=4096" in parts[1] and "along/across" in parts[1]
+        assert lib.gb_set_multipass_levels(3) == 0
+        assert lib.gb_set_fused_passes(0) == 0
+        parts = _sched(lib, 1 << 24, 0).split("; ")
+        assert len(parts) == 3
+        assert all("L=256" in p for p in parts)
+        assert "epi=twiddle" in parts[0] and "epi=twiddle" in parts[1]
+        assert "along/across" in parts[2] and "grid=16x256" in parts[2]
+        assert lib.gb_set_fused_passes(1) == 0
+        parts = _sched(lib, 1 << 24, 0).split("; ")
+        assert len(parts) == 2 and "L=256" in parts[0] and parts[1].startswith("fused_bc")
+        assert "blocks=16 ring=4" in parts[1]
+        assert lib.gb_set_multipass_levels(5) == -1
+        lib.gb_clear_error()
+    finally:
+        lib.gb_set_multipass_levels(0)
+        lib.gb_set_fused_passes(0)
     s = _sched(lib, 1 << 21, 1)  # r2c of 2^21 reals = 2^20 complex + in-place fix-up
     assert s.split("; ")[-1].startswith("r2c_fixup")
