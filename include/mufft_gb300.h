@@ -71,6 +71,40 @@ int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, cons
 int mufft_gb_execute_plan_1d_launches_async(mufft_plan_1d *plan, void *output, const void *input,
                                             unsigned first, unsigned count, void *stream);
 
+/* --------------------------------------------- ragged batched convolution */
+
+/* No counterpart in the reference, which convolves one block per call
+ * (fft.c:794-809).  One request is what mufft_execute_conv_input(FIRST) +
+ * mufft_execute_conv_output do for one block: transform `input`, multiply by
+ * the already transformed second block `filter` (from
+ * mufft_execute_conv_input(SECOND) of a plan of the same N and method), scale
+ * by 1/N and transform back into `output`.
+ *   N: power of two; MONO_MONO 32..65536, STEREO_MONO 16..65536.
+ *   method: MUFFT_CONV_METHOD_FLAG_* (ZERO_PAD_UPPER_HALF_FIRST: input has N/2
+ *     samples; the SECOND flag was applied when the filter was transformed).
+ *   input: N (N/2) floats for mono, N (N/2) complex for stereo; filter: N/2+1
+ *     (mono) or N (stereo) complex; output: N floats / N complex.  Device
+ *     memory; the addresses are fixed when the batch is created. */
+typedef struct mufft_gb_conv_request {
+    unsigned N;
+    unsigned method;
+    const void *input;
+    const void *filter;
+    void *output;
+} mufft_gb_conv_request;
+
+typedef struct mufft_gb_conv_batch mufft_gb_conv_batch;
+
+/* Prepares `count` requests of mixed sizes for one persistent launch (requests
+ * ordered longest first, each run by one CTA), captured in a CUDA graph.
+ * flags: 0. */
+mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *requests, unsigned count,
+                                                unsigned flags);
+/* Replays the batch on `stream` (enqueued, not synchronised).  Executes of one
+ * batch must not overlap on the GPU (they share its scratch). */
+int mufft_gb_execute_conv_batch(mufft_gb_conv_batch *batch, void *stream);
+void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch);
+
 /* ------------------------------------------------- allocation-free execute */
 
 /* No counterpart in the reference.  A forward or inverse c2c transform of N

@@ -84,6 +84,9 @@ GB_H = [
     ("set_fused_passes", _i, [_i]),
     ("list_tiles", _i, [C.c_char_p, _sz]),
     ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
+    ("create_conv_batch", _vp, [_vp, _u, _u]),
+    ("execute_conv_batch", _i, [_vp, _vp]),
+    ("free_conv_batch", None, [_vp]),
     ("device_alloc", _vp, [_sz]),
     ("device_free", None, [_vp]),
     ("memcpy", _i, [_vp, _vp, _sz]),
@@ -91,6 +94,12 @@ GB_H = [
 ]
 
 CONVOLVE_FUNC = C.CFUNCTYPE(None, _vp, _vp, _vp, C.c_float, _u)
+
+
+class ConvRequest(C.Structure):
+    """mufft_gb_conv_request (include/mufft_gb300.h)."""
+    _fields_ = [("N", C.c_uint), ("method", C.c_uint), ("input", C.c_void_p), ("filter", C.c_void_p),
+                ("output", C.c_void_p)]
 
 
 class MuFFTError(RuntimeError):

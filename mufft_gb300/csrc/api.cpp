@@ -20,6 +20,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -29,6 +30,7 @@
 #include "../../include/mufft_gb300.h"
 #include "bc_fused.h"
 #include "common.h"
+#include "conv_ragged.h"
 #include "misc_kernels.h"
 #include "registry.h"
 
@@ -1270,6 +1272,182 @@ extern "C" mufft_convolve_func mufft_get_convolve_func(unsigned flags)
     (void)flags;
     return &gpu_convolve;
 }
+
+// ================================================================ ragged conv
+
+struct mufft_gb_conv_batch {
+    int device = -1;
+    unsigned count = 0;
+    RaggedReq *d_reqs = nullptr;
+    unsigned *d_next = nullptr;
+    float2 *d_scratch = nullptr;
+    float2 *d_rtw = nullptr;
+    cudaStream_t capture = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned grid = 0;
+};
+
+namespace {
+
+void destroy_conv_batch(mufft_gb_conv_batch *b)
+{
+    if (!b)
+        return;
+    if (b->device >= 0) {
+        DeviceGuard g(b->device);
+        if (b->exec)
+            cudaGraphExecDestroy(b->exec);
+        if (b->graph)
+            cudaGraphDestroy(b->graph);
+        if (b->capture)
+            cudaStreamDestroy(b->capture);
+        cudaFree(b->d_reqs);
+        cudaFree(b->d_next);
+        cudaFree(b->d_scratch);
+        cudaFree(b->d_rtw);
+    }
+    delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *requests, unsigned count,
+                                                unsigned flags)
+{
+    (void)flags;
+    t_err = 0;
+    if (!requests || count == 0) {
+        set_error(MUFFT_GB_ERR_INVALID, "no requests");
+        return nullptr;
+    }
+    std::vector<RaggedReq> reqs(count);
+    std::vector<unsigned long long> cost(count);
+    bool need[17] = {};
+    size_t scratch_elems = 0;
+    std::vector<size_t> spec_off(count);
+    for (unsigned i = 0; i < count; i++) {
+        const mufft_gb_conv_request &r = requests[i];
+        const bool stereo = (r.method & 1u) == MUFFT_CONV_METHOD_FLAG_STEREO_MONO;
+        if (!is_pow2(r.N) || !r.input || !r.filter || !r.output) {
+            set_error(MUFFT_GB_ERR_INVALID, "request %u: N must be a power of two and buffers non-null", i);
+            return nullptr;
+        }
+        const unsigned L = stereo ? r.N : r.N / 2;
+        const unsigned lg = ilog2u(L);
+        if (L < 16 || L > 65536) {
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "request %u: N=%u outside the ragged range", i, r.N);
+            return nullptr;
+        }
+        RaggedReq &q = reqs[i];
+        q.in = (const float2 *)r.input;
+        q.h = (const float2 *)r.filter;
+        q.out = (float2 *)r.output;
+        q.scale = 1.0f / (float)r.N;
+        q.lg = lg;
+        q.stereo = stereo ? 1 : 0;
+        q.zero_pad = (r.method & MUFFT_CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST) ? 1 : 0;
+        need[lg] = true;
+        cost[i] = (unsigned long long)L * lg;
+        spec_off[i] = scratch_elems;
+        scratch_elems += ((size_t)L + 1 + 31) & ~(size_t)31;  // 256-byte aligned slots
+    }
+    int dev;
+    if (!device_prepare(&dev))
+        return nullptr;
+    mufft_gb_conv_batch *b = new mufft_gb_conv_batch();
+    b->device = dev;
+    b->count = count;
+    RaggedArgs args{};
+    // per-size r2c / c2r fix-up twiddles, FP64 then rounded (fft.c:441-455)
+    std::vector<float2> rtw;
+    for (unsigned lg = 0; lg <= 16; lg++) {
+        args.rtw_off[lg] = (unsigned)rtw.size();
+        if (!need[lg])
+            continue;
+        std::vector<float2> f = r2c_twiddles(MUFFT_FORWARD, 1u << lg), iv = r2c_twiddles(MUFFT_INVERSE, 1u << lg);
+        rtw.insert(rtw.end(), f.begin(), f.end());
+        rtw.insert(rtw.end(), iv.begin(), iv.end());
+    }
+    if (rtw.empty())
+        rtw.push_back(make_float2(0.f, 0.f));
+    b->d_rtw = upload(rtw);
+    if (!b->d_rtw || !cuda_ok(cudaMalloc(&b->d_scratch, scratch_elems * sizeof(float2)), "cudaMalloc(scratch)") ||
+        !cuda_ok(cudaMalloc(&b->d_next, sizeof(unsigned)), "cudaMalloc(counter)") ||
+        !cuda_ok(cudaMalloc(&b->d_reqs, count * sizeof(RaggedReq)), "cudaMalloc(requests)")) {
+        destroy_conv_batch(b);
+        return nullptr;
+    }
+    // longest first (LPT), so the largest requests start at once
+    std::vector<unsigned> order(count);
+    for (unsigned i = 0; i < count; i++)
+        order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](unsigned x, unsigned y) { return cost[x] > cost[y]; });
+    std::vector<RaggedReq> sorted(count);
+    for (unsigned i = 0; i < count; i++) {
+        sorted[i] = reqs[order[i]];
+        sorted[i].spec = b->d_scratch + spec_off[order[i]];
+    }
+    if (!cuda_ok(cudaMemcpy(b->d_reqs, sorted.data(), count * sizeof(RaggedReq), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(requests)")) {
+        destroy_conv_batch(b);
+        return nullptr;
+    }
+    const size_t smem = conv_ragged_smem();
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (!cuda_ok(cudaFuncSetAttribute(conv_ragged_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "cudaFuncSetAttribute") ||
+        !cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_ragged_fn(), conv_ragged_threads(), smem),
+                 "occupancy")) {
+        destroy_conv_batch(b);
+        return nullptr;
+    }
+    b->grid = (unsigned)(sms * std::max(per_sm, 1));
+    if (b->grid > count)
+        b->grid = count;
+    args.reqs = b->d_reqs;
+    args.count = count;
+    args.next = b->d_next;
+    args.tw = g_dev[dev].tw;
+    args.rtw = b->d_rtw;
+    // capture counter reset + the persistent launch once; executes replay the graph
+    void *kargs[] = {&args};
+    bool ok = cuda_ok(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "cudaStreamCreate") &&
+              cuda_ok(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "capture") &&
+              cuda_ok(cudaMemsetAsync(b->d_next, 0, sizeof(unsigned), b->capture), "cudaMemsetAsync") &&
+              cuda_ok(cudaLaunchKernel(conv_ragged_fn(), dim3(b->grid), dim3(conv_ragged_threads()), kargs, smem,
+                                       b->capture),
+                      "kernel launch");
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(b->capture, &g);
+    if (!ok || !cuda_ok(ce, "capture") || !cuda_ok(cudaGraphInstantiate(&b->exec, g, 0), "cudaGraphInstantiate")) {
+        if (g)
+            cudaGraphDestroy(g);
+        destroy_conv_batch(b);
+        return nullptr;
+    }
+    b->graph = g;
+    return b;
+}
+
+int mufft_gb_execute_conv_batch(mufft_gb_conv_batch *batch, void *stream)
+{
+    if (!batch) {
+        set_error(MUFFT_GB_ERR_INVALID, "null batch");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(batch->device);
+    if (!cuda_ok(cudaGraphLaunch(batch->exec, (cudaStream_t)stream), "cudaGraphLaunch"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch) { destroy_conv_batch(batch); }
+
+}  // extern "C"
 
 // ================================================================== 2D
 

@@ -1,0 +1,230 @@
+// Ragged batched fast convolution: many muFFT convolution requests of mixed
+// power-of-two sizes in one persistent launch.
+//
+// A request is the reference's per-block convolution (fft.c:794-809): the
+// first block is transformed (zero-padded input allowed), multiplied by the
+// already transformed second block (a filter spectrum from
+// mufft_execute_conv_input), scaled by 1/N and transformed back.  MONO_MONO
+// goes through an N/2-point complex FFT with the r2c/c2r fix-ups,
+// STEREO_MONO through an N-point complex FFT (fft.c:585-599).
+//
+// Every CTA (512 threads) takes the next request from a global counter, the
+// host having sorted requests longest first, and runs it alone:
+//   L <= 8192 complex points: one forward tile (r2c fix-up fused into its
+//     store for mono) writes the spectrum to the request's scratch, which
+//     stays in L2; one inverse tile reads it back with the multiply and the
+//     c2r pre-pass fused into its loads.
+//   L = 16384 .. 65536: an in-CTA four-step over the request's scratch,
+//     L = L1 x L2.  The forward half stops at the transposed spectrum
+//     X^T[k1][k2] = X[k1 + L1*k2] (no transpose), the multiply (and for mono
+//     the r2c fix-up, product and c2r pre-pass of each bin pair k, L-k) runs
+//     on that layout, and the inverse four-step consumes it directly:
+//       F1 columns of L1 with W_L^(n2*k1) -> F2 rows of L2 -> multiply ->
+//       I1 rows of L2 (inverse) with W_L^(-n2*k1) -> I2 columns of L1 -> output.
+#include "../../include/fft.h"
+#include "conv_ragged.h"
+#include "fft_device.cuh"
+
+namespace mgb {
+
+namespace {
+
+constexpr int kThreads = 512;
+
+template <int L> __host__ __device__ constexpr int single_c() { return kThreads * 16 / L; }
+
+// Forward tile into the spectrum scratch, then the fused multiply + inverse
+// tile into the output.
+template <int L>
+__device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
+                            const float2 *rtw_inv)
+{
+    constexpr int C = single_c<L>();
+    const bool mono = q.stereo == 0;
+    TileArgs f{};
+    f.in = q.in;
+    f.out = q.spec;
+    f.in_stride = f.out_stride = 1;
+    f.in_dist = f.out_dist = L + 1;
+    f.ntrans = 1;
+    f.half = q.zero_pad;
+    f.epilogue = mono ? EPI_R2C : EPI_PLAIN;
+    f.tw = tw;
+    f.rtw = rtw_fwd;
+    f.scale = 1.0f;
+    tile_body<L, 16, C, 1, ALONG, ALONG, false>(f, 0, 0, 0, 0, smem);
+    __syncthreads();  // spectrum complete and visible to the whole CTA
+
+    TileArgs b{};
+    b.in = q.spec;
+    b.in2 = q.h;
+    b.out = q.out;
+    b.in_stride = b.out_stride = 1;
+    b.in_dist = b.out_dist = L + 1;
+    b.ntrans = 1;
+    b.prologue = mono ? PRO_MUL_C2R : PRO_MUL;
+    b.mirror_len = L;
+    b.rtw = rtw_inv;
+    b.scale = q.scale;
+    b.conj = 3;
+    b.tw = tw;
+    tile_body<L, 16, C, 1, ALONG, ALONG, true>(b, 0, 0, 0, 0, smem);
+    __syncthreads();
+}
+
+// Multiply phase of the four-step path on the transposed spectrum.
+template <int L1, int L2>
+__device__ void conv_multiply(const RaggedReq &q, const float2 *rtw_fwd, const float2 *rtw_inv)
+{
+    constexpr int L = L1 * L2;
+    float2 *s = q.spec;
+    auto at = [](int k) { return (k % L1) * L2 + k / L1; };  // X[k] lives at X^T[k % L1][k / L1]
+    if (q.stereo) {
+        for (int idx = threadIdx.x; idx < L; idx += kThreads) {
+            const int k = (idx / L2) + L1 * (idx % L2);
+            s[idx] = cscale(cmul(__ldcg(&s[idx]), __ldcg(&q.h[k])), q.scale);
+        }
+        return;
+    }
+    // mono: Z (forward complex FFT of the packed reals) -> r2c bins X -> Y = s*X*H
+    // -> c2r pre-pass Zi, pair by pair (kernel.c:36-82).
+    for (int k = threadIdx.x; k <= L / 2; k += kThreads) {
+        if (k == 0) {
+            const float2 z0 = __ldcg(&s[0]);
+            const float2 x0 = make_float2(z0.x + z0.y, 0.f), xm = make_float2(z0.x - z0.y, 0.f);
+            const float2 y0 = cscale(cmul(x0, __ldcg(&q.h[0])), q.scale);
+            const float2 ym = cscale(cmul(xm, __ldcg(&q.h[L])), q.scale);
+            s[0] = c2r_fixup(y0, ym, __ldg(&rtw_inv[0]));
+            continue;
+        }
+        const int km = L - k;
+        const int ik = at(k), im = at(km);
+        const float2 zk = __ldcg(&s[ik]), zm = __ldcg(&s[im]);
+        float2 xk, xk_hi, xm, xm_hi;
+        r2c_bins(zk, zm, __ldg(&rtw_fwd[k]), xk, xk_hi);
+        r2c_bins(zm, zk, __ldg(&rtw_fwd[km]), xm, xm_hi);
+        const float2 yk = cscale(cmul(xk, __ldcg(&q.h[k])), q.scale);
+        const float2 ym = cscale(cmul(xm, __ldcg(&q.h[km])), q.scale);
+        s[ik] = c2r_fixup(yk, ym, __ldg(&rtw_inv[k]));
+        if (km != k)
+            s[im] = c2r_fixup(ym, yk, __ldg(&rtw_inv[km]));
+    }
+}
+
+template <int L1, int L2>
+__device__ void conv_multi(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
+                           const float2 *rtw_inv)
+{
+    constexpr int L = L1 * L2;
+    constexpr int C1 = kThreads * 16 / L1, C2 = kThreads * 16 / L2;
+    TileArgs a{};
+    a.tw = tw;
+    a.scale = 1.0f;
+    a.tw_scale = 2.0f / (float)L;
+    a.tw_mask = L - 1;
+
+    // F1: columns of length L1 (n1), stride L2, twiddle W_L^(k1*n2)
+    TileArgs f1 = a;
+    f1.in = q.in;
+    f1.out = q.spec;
+    f1.in_stride = f1.out_stride = L2;
+    f1.in_dist = f1.out_dist = 1;
+    f1.ntrans = L2;
+    f1.half = q.zero_pad;
+    f1.epilogue = EPI_TWIDDLE;
+    for (int t = 0; t < L2 / C1; t++)
+        tile_body<L1, 16, C1, 1, ACROSS, ACROSS, false>(f1, t, 0, 0, 0, smem);
+    __syncthreads();
+    // F2: rows of length L2, in place -> X^T[k1][k2]
+    TileArgs f2 = a;
+    f2.in = q.spec;
+    f2.out = q.spec;
+    f2.in_stride = f2.out_stride = 1;
+    f2.in_dist = f2.out_dist = L2;
+    f2.ntrans = L1;
+    for (int t = 0; t < L1 / C2; t++)
+        tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(f2, t, 0, 0, 0, smem);
+    __syncthreads();
+    conv_multiply<L1, L2>(q, rtw_fwd, rtw_inv);
+    __syncthreads();
+    // I1: rows, inverse over k2: conj in, forward FFT, W_L^(n2*k1) -> conj(Z)
+    TileArgs i1 = f2;
+    i1.conj = 1;
+    i1.epilogue = EPI_TWIDDLE;
+    for (int t = 0; t < L1 / C2; t++)
+        tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(i1, t, 0, 0, 0, smem);
+    __syncthreads();
+    // I2: columns, inverse over k1 of conj(Z): forward FFT, conj out -> natural output
+    TileArgs i2 = a;
+    i2.in = q.spec;
+    i2.out = q.out;
+    i2.in_stride = i2.out_stride = L2;
+    i2.in_dist = i2.out_dist = 1;
+    i2.ntrans = L2;
+    i2.conj = 2;
+    for (int t = 0; t < L2 / C1; t++)
+        tile_body<L1, 16, C1, 1, ACROSS, ACROSS, true>(i2, t, 0, 0, 0, smem);
+    __syncthreads();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedArgs args)
+{
+    extern __shared__ float2 smem[];
+    __shared__ unsigned s_idx;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_idx = atomicAdd(args.next, 1u);
+        __syncthreads();
+        const unsigned i = s_idx;
+        __syncthreads();
+        if (i >= args.count)
+            return;
+        const RaggedReq q = args.reqs[i];
+        const float2 *rf = args.rtw + args.rtw_off[q.lg];
+        const float2 *ri = rf + (1u << q.lg);
+        switch (q.lg) {
+        case 4: conv_single<16>(q, smem, args.tw, rf, ri); break;
+        case 5: conv_single<32>(q, smem, args.tw, rf, ri); break;
+        case 6: conv_single<64>(q, smem, args.tw, rf, ri); break;
+        case 7: conv_single<128>(q, smem, args.tw, rf, ri); break;
+        case 8: conv_single<256>(q, smem, args.tw, rf, ri); break;
+        case 9: conv_single<512>(q, smem, args.tw, rf, ri); break;
+        case 10: conv_single<1024>(q, smem, args.tw, rf, ri); break;
+        case 11: conv_single<2048>(q, smem, args.tw, rf, ri); break;
+        case 12: conv_single<4096>(q, smem, args.tw, rf, ri); break;
+        case 13: conv_single<8192>(q, smem, args.tw, rf, ri); break;
+        case 14: conv_multi<128, 128>(q, smem, args.tw, rf, ri); break;
+        case 15: conv_multi<128, 256>(q, smem, args.tw, rf, ri); break;
+        case 16: conv_multi<256, 256>(q, smem, args.tw, rf, ri); break;
+        default: break;
+        }
+    }
+}
+
+template <int L> constexpr size_t single_bytes() { return tile_exchange_bytes<L, 16, single_c<L>(), 1, ALONG, ALONG>(); }
+template <int L1, int L2> constexpr size_t multi_bytes()
+{
+    constexpr size_t a = tile_exchange_bytes<L1, 16, kThreads * 16 / L1, 1, ACROSS, ACROSS>();
+    constexpr size_t b = tile_exchange_bytes<L2, 16, kThreads * 16 / L2, 1, ALONG, ALONG>();
+    return a > b ? a : b;
+}
+
+size_t conv_ragged_smem()
+{
+    // every tile conv_ragged_kernel instantiates
+    const size_t v[] = {single_bytes<16>(),   single_bytes<32>(),   single_bytes<64>(),   single_bytes<128>(),
+                        single_bytes<256>(),  single_bytes<512>(),  single_bytes<1024>(), single_bytes<2048>(),
+                        single_bytes<4096>(), single_bytes<8192>(), multi_bytes<128, 128>(),
+                        multi_bytes<128, 256>(), multi_bytes<256, 256>()};
+    size_t m = 0;
+    for (size_t x : v)
+        m = x > m ? x : m;
+    return m;
+}
+
+const void *conv_ragged_fn() { return (const void *)&conv_ragged_kernel; }
+int conv_ragged_threads() { return kThreads; }
+
+}  // namespace mgb

@@ -108,6 +108,23 @@ def test_valid_plan_without_gpu_reports_no_device(lib):
     lib.gb_clear_error()
 
 
+def test_conv_batch_validates_requests_on_host(lib):
+    """Request checks run before any device work (no GPU needed)."""
+    fake = 0x10000
+    cases = [(1000, 0, (fake, fake, fake), -1), (1 << 18, 0, (fake, fake, fake), -2),
+             (16, 0, (fake, fake, fake), -2), (1 << 17, K.CONV_METHOD_FLAG_STEREO_MONO, (fake, fake, fake), -2),
+             (1024, 0, (fake, None, fake), -1)]
+    for N, method, ptrs, code in cases:
+        reqs = (K.ConvRequest * 1)(K.ConvRequest(N, method, *ptrs))
+        assert not lib.gb_create_conv_batch(reqs, 1, 0)
+        assert lib.gb_last_error() == code, (N, method)
+        lib.gb_clear_error()
+    assert not lib.gb_create_conv_batch(None, 0, 0)
+    assert lib.gb_last_error() == -1
+    lib.gb_clear_error()
+    lib.gb_free_conv_batch(None)
+
+
 def _sched(lib, N, kind, direction=K.FORWARD, flags=0, batch=1):
     buf = C.create_string_buffer(4096)
     rc = lib.gb_describe_schedule_1d(N, kind, direction, flags, batch, buf, 4096)

@@ -1,0 +1,174 @@
+"""GPU tests of the ragged batched convolution (mufft_gb_create_conv_batch):
+requests of mixed sizes and methods in one persistent launch, each checked
+against the oracle's full convolution sequence (fft.c:794-809) and against
+the single-request plan path."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import REL_L2_TOL, direct_conv_f64, rel_l2
+from mufft_gb300 import capi as K
+from mufft_gb300 import signals
+
+pytestmark = pytest.mark.gpu
+
+STEREO = K.CONV_METHOD_FLAG_STEREO_MONO
+PAD1 = K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST
+PAD2 = K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import mufft_gb300
+    return mufft_gb300.load()
+
+
+@pytest.fixture(scope="module")
+def ora():
+    from oracle.oracle import load_oracle
+    return load_oracle()
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available()
+    return t
+
+
+def filter_spectrum(gpu, b: np.ndarray, N: int, method: int) -> np.ndarray:
+    """Second block transformed by mufft_execute_conv_input(SECOND)."""
+    plan = gpu.create_plan_conv(N, 0, method)
+    assert plan, gpu.gb_last_error_string()
+    try:
+        nblk = gpu.conv_get_transformed_block_size(plan) // 8
+        out = K.aligned_zeros(nblk, np.complex64)
+        src = K.aligned_copy(b, np.float32)
+        gpu.execute_conv_input(plan, K.CONV_BLOCK_SECOND, out.ctypes.data, src.ctypes.data)
+        gpu.check("conv_input")
+    finally:
+        gpu.free_plan_conv(plan)
+    return out
+
+
+class Batch:
+    """Device buffers and the batch handle for a list of (N, method) requests."""
+
+    def __init__(self, gpu, torch, specs, seed):
+        self.gpu, self.specs = gpu, specs
+        self.a, self.b, self.din, self.dh, self.dout = [], [], [], [], []
+        reqs = (K.ConvRequest * len(specs))()
+        for i, (N, method) in enumerate(specs):
+            stereo = (method & 1) == STEREO
+            a = (signals.complex_uniform(seed + 2 * i, N) if stereo else signals.uniform(seed + 2 * i, N))
+            b = signals.uniform(seed + 2 * i + 1, N)
+            H = filter_spectrum(gpu, b, N, method)
+            din = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+            dh = torch.from_numpy(H).cuda()
+            dout = torch.full((N,), float("nan"), dtype=torch.complex64 if stereo else torch.float32, device="cuda")
+            reqs[i] = K.ConvRequest(N, method, din.data_ptr(), dh.data_ptr(), dout.data_ptr())
+            self.a.append(a), self.b.append(b), self.din.append(din), self.dh.append(dh), self.dout.append(dout)
+        self.handle = gpu.gb_create_conv_batch(reqs, len(specs), 0)
+        assert self.handle, gpu.gb_last_error_string()
+
+    def run(self, torch):
+        rc = self.gpu.gb_execute_conv_batch(self.handle, torch.cuda.current_stream().cuda_stream)
+        assert rc == 0, self.gpu.gb_last_error_string()
+        torch.cuda.synchronize()
+        return [d.cpu().numpy() for d in self.dout]
+
+    def free(self):
+        self.gpu.gb_free_conv_batch(self.handle)
+
+
+def _mixed_specs(rng_seed: int, count: int):
+    rng = np.random.default_rng(rng_seed)
+    specs = []
+    for _ in range(count):
+        method = int(rng.choice([0, STEREO, PAD1, STEREO | PAD1, PAD2, STEREO | PAD1 | PAD2]))
+        stereo = method & 1
+        lg = int(rng.integers(4, 17)) + (0 if stereo else 1)  # complex length 2^4 .. 2^16
+        specs.append((1 << lg, method))
+    return specs
+
+
+def test_conv_batch_mixed_sizes_vs_oracle(gpu, ora, torch):
+    specs = _mixed_specs(7, 48)
+    # every kernel branch at least once: complex lengths 16 .. 65536, mono and stereo
+    specs += [(1 << (lg + 1), 0) for lg in range(4, 17)] + [(1 << lg, STEREO) for lg in range(4, 17)]
+    bt = Batch(gpu, torch, specs, 90000)
+    try:
+        outs = bt.run(torch)
+    finally:
+        bt.free()
+    for i, ((N, method), got) in enumerate(zip(specs, outs)):
+        want = ora.conv(bt.a[i], bt.b[i], N, method)
+        assert np.all(np.isfinite(got)), (i, N, method)
+        assert rel_l2(got, want) <= REL_L2_TOL, (i, N, method, rel_l2(got, want))
+
+
+@pytest.mark.parametrize("method", [0, STEREO, PAD1 | PAD2, STEREO | PAD1 | PAD2])
+def test_conv_batch_vs_direct_fp64(gpu, torch, method):
+    """Zero-padded blocks make the circular convolution a linear one; check
+    against the FP64 direct sum."""
+    specs = [(N, method) for N in (64, 1024, 8192, 32768, 131072 if not method & 1 else 65536)]
+    bt = Batch(gpu, torch, specs, 91000 + method)
+    try:
+        outs = bt.run(torch)
+    finally:
+        bt.free()
+    for i, (N, m) in enumerate(specs):
+        a = bt.a[i].copy()
+        b = bt.b[i].copy()
+        if m & PAD1:
+            a[N // 2:] = 0
+        if m & PAD2:
+            b[N // 2:] = 0
+        ref = direct_conv_f64(a, b, N) if N <= 8192 else np.fft.ifft(
+            np.fft.fft(a.astype(np.complex128)) * np.fft.fft(b.astype(np.float64)))
+        if not m & 1:
+            ref = np.real(ref)
+        assert rel_l2(outs[i], ref) < 2e-6, (N, m)
+
+
+def test_conv_batch_matches_single_plans(gpu, torch):
+    """The batch computes what the per-request plan path computes."""
+    specs = [(4096, 0), (65536, STEREO), (256, PAD1), (131072, PAD1 | PAD2)]
+    bt = Batch(gpu, torch, specs, 92000)
+    try:
+        outs = bt.run(torch)
+    finally:
+        bt.free()
+    for i, (N, m) in enumerate(specs):
+        single = gpu.conv(bt.a[i], bt.b[i], N, m)
+        assert rel_l2(outs[i], single) < 1e-6, (N, m)
+
+
+def test_conv_batch_replay_is_deterministic(gpu, torch):
+    specs = _mixed_specs(11, 300)
+    bt = Batch(gpu, torch, specs, 93000)
+    try:
+        first = bt.run(torch)
+        for d in bt.dout:
+            d.fill_(float("nan"))
+        second = bt.run(torch)
+    finally:
+        bt.free()
+    for x, y in zip(first, second):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_conv_batch_rejects_bad_requests(gpu, torch):
+    d = torch.zeros(1 << 18, dtype=torch.float32, device="cuda")
+    p = d.data_ptr()
+    for N, method, ptrs in [(1000, 0, (p, p, p)), (1 << 18, 0, (p, p, p)), (16, 0, (p, p, p)),
+                            (1 << 17, STEREO, (p, p, p)), (1024, 0, (p, None, p))]:
+        reqs = (K.ConvRequest * 1)(K.ConvRequest(N, method, *ptrs))
+        assert not gpu.gb_create_conv_batch(reqs, 1, 0)
+        assert gpu.gb_last_error() in (-1, -2), (N, method)
+        gpu.gb_clear_error()
+    assert not gpu.gb_create_conv_batch(None, 0, 0)
+    gpu.gb_clear_error()
