@@ -71,6 +71,37 @@ int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, cons
 int mufft_gb_execute_plan_1d_launches_async(mufft_plan_1d *plan, void *output, const void *input,
                                             unsigned first, unsigned count, void *stream);
 
+/* ------------------------------------------------- convolution adjoints */
+
+/* No counterpart in the reference.  Gradients of a convolution plan's output
+ * out = (1/N) IFFT(FFT(first) . FFT(second)) (mufft_execute_conv_output,
+ * fft.c:794-809) for an upstream gradient `grad_output` of `out` (N reals for
+ * MONO_MONO, N complex for STEREO_MONO; full length, never zero-padded).
+ * Complex gradients follow the dL/dRe + i dL/dIm convention.  Device
+ * buffers; enqueued on `stream`; calls on one plan must not overlap (they
+ * share its scratch).  The first call of each allocates the plan's adjoint
+ * transforms and scratch. */
+
+/* d out / d first, applied to grad_output:
+ *   grad_input = (1/N) IFFT(FFT(grad_output) . conj(second_spectrum))
+ * second_spectrum: the transformed second block (mufft_execute_conv_input
+ * with MUFFT_CONV_BLOCK_SECOND).  grad_input: N reals (mono) / N complex
+ * (stereo); with ZERO_PAD_UPPER_HALF_FIRST only its first N/2 entries belong
+ * to real inputs. */
+int mufft_gb_conv_adjoint_input(mufft_plan_conv *plan, void *grad_input, const void *grad_output,
+                                const void *second_spectrum, void *stream);
+
+/* d out / d second, summed over `batch` signals that share the second block:
+ *   grad_filter = Re (1/N) IFFT(sum_b FFT(grad_output_b) . conj(first_spectrum_b))
+ * The sum runs over spectra (one inverse transform in all).  grad_outputs:
+ * batch blocks `output_dist` samples apart (floats for mono, complex for
+ * stereo); first_spectra: the transformed first blocks (MUFFT_CONV_BLOCK_FIRST)
+ * `spectrum_dist` complex apart.  grad_filter: N reals; with
+ * ZERO_PAD_UPPER_HALF_SECOND only its first N/2 entries belong to taps. */
+int mufft_gb_conv_adjoint_filter(mufft_plan_conv *plan, float *grad_filter, const void *grad_outputs,
+                                 size_t output_dist, const void *first_spectra, size_t spectrum_dist,
+                                 unsigned batch, void *stream);
+
 /* --------------------------------------------- ragged batched convolution */
 
 /* No counterpart in the reference, which convolves one block per call

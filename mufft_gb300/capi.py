@@ -84,6 +84,8 @@ GB_H = [
     ("set_fused_passes", _i, [_i]),
     ("list_tiles", _i, [C.c_char_p, _sz]),
     ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
+    ("conv_adjoint_input", _i, [_vp, _vp, _vp, _vp, _vp]),
+    ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),
     ("free_conv_batch", None, [_vp]),

@@ -393,6 +393,7 @@ struct FftSpec {
     int conj_in = 0, conj_out = 0;
     Role in_role = ROLE_IN, out_role = ROLE_OUT, in2_role = ROLE_NONE;
     float scale = 1.0f;
+    int conj2 = 0;                        // multiply by conj(in2): adjoint convolution
 };
 
 // Device tables and scratch a schedule needs; allocated unless `dry`.
@@ -503,6 +504,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
         p.in_role = s.in_role;
         p.out_role = s.out_role;
         p.in2_role = s.in2_role;
+        p.a.conj2 = s.conj2;
         p.grid = dim3((s.batch + k->C - 1) / k->C, 1);
         out.push_back(p);
         return true;
@@ -594,6 +596,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
             pa.a.scale = s.scale;
             pa.in_role = s.in_role;
             pa.in2_role = s.in2_role;
+            pa.a.conj2 = s.conj2;
             pa.out_role = ROLE_SCRATCH;
             pa.grid = dim3((unsigned)((MR + ka->C - 1) / ka->C), s.batch);
             out.push_back(pa);
@@ -655,6 +658,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
         pa.a.scale = s.scale;
         pa.in_role = s.in_role;
         pa.in2_role = s.in2_role;
+        pa.a.conj2 = s.conj2;
         pa.out_role = ROLE_SCRATCH;
         pa.grid = dim3((unsigned)((MR + ka->C - 1) / ka->C), s.batch);
         out.push_back(pa);
@@ -747,6 +751,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p1.a.tw_lo = use_twiddle_table(kc) ? res.twlo : nullptr;
     p1.in_role = s.in_role;
     p1.in2_role = s.in2_role;
+    p1.a.conj2 = s.conj2;
     p1.out_role = ROLE_SCRATCH;
     p1.grid = dim3((N2 + kc->C - 1) / kc->C, s.batch);
     out.push_back(p1);
@@ -855,7 +860,7 @@ void destroy_1d(mufft_plan_1d *pl)
 // prologue_override: PRO_MUL / PRO_MUL_C2R for convolution output plans.
 mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, unsigned batch,
                          size_t idist, size_t odist, int prologue_override, bool dry,
-                         std::string *desc)
+                         std::string *desc, bool conj2 = false)
 {
     t_err = 0;
     if (!is_pow2(N) || N == 1) {
@@ -918,6 +923,7 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
     if (prologue_override >= 0) {
         s.prologue = prologue_override;
         s.in2_role = ROLE_IN2;
+        s.conj2 = conj2 ? 1 : 0;
         pl->uses_in2 = true;
     }
     // r2c input of N reals is read as M complex pairs.
@@ -1134,6 +1140,17 @@ struct mufft_plan_conv {
     size_t block_size = 0;
     mufft_plan_1d *in_plan[2] = {nullptr, nullptr};
     mufft_plan_1d *out_plan = nullptr;
+    // adjoints (mufft_gb_conv_adjoint_*), made on first use
+    int device = -1;
+    mufft_plan_1d *adj_fwd = nullptr;        // gradient of the output -> spectrum (full length)
+    mufft_plan_1d *adj_mul = nullptr;        // x conj(second spectrum), 1/N, inverse
+    mufft_plan_1d *adj_fwd_batch = nullptr;  // the forward transform over a chunk of gradients
+    unsigned adj_chunk = 0;
+    size_t adj_dist = 0;
+    mufft_plan_1d *adj_c2r = nullptr;        // N/2 + 1 bins -> N reals
+    float2 *adj_spec = nullptr;              // spectra of the gradients
+    size_t adj_spec_bytes = 0;
+    float2 *adj_acc = nullptr;               // N/2 + 1 bins of the filter gradient
 };
 
 extern "C" {
@@ -1168,6 +1185,7 @@ mufft_plan_conv *mufft_create_plan_conv(unsigned N, unsigned flags, unsigned met
         mufft_free_plan_conv(c);
         return nullptr;
     }
+    c->device = c->out_plan->device;
     return c;
 }
 
@@ -1219,7 +1237,151 @@ void mufft_free_plan_conv(mufft_plan_conv *plan)
     destroy_1d(plan->in_plan[0]);
     destroy_1d(plan->in_plan[1]);
     destroy_1d(plan->out_plan);
+    destroy_1d(plan->adj_fwd);
+    destroy_1d(plan->adj_mul);
+    destroy_1d(plan->adj_fwd_batch);
+    destroy_1d(plan->adj_c2r);
+    if (plan->device >= 0) {
+        DeviceGuard g(plan->device);
+        cudaFree(plan->adj_spec);
+        cudaFree(plan->adj_acc);
+    }
     delete plan;
+}
+
+}  // extern "C"
+
+// ============================================================ conv adjoint
+//
+// For out = (1/N) IFFT(FFT(first) . FFT(second)) (fft.c:794-809) and an
+// upstream gradient G_out of `out`:
+//   d/d first  = (1/N) IFFT(FFT(G_out) . conj(FFT(second)))
+//   d/d second = Re (1/N) IFFT(sum_b FFT(G_out_b) . conj(FFT(first_b)))
+// (complex gradients in the d/dRe + i d/dIm convention; the second block is
+// real in both conv methods).
+
+namespace {
+
+bool conv_stereo(const mufft_plan_conv *c) { return (c->method & 1u) == MUFFT_CONV_METHOD_FLAG_STEREO_MONO; }
+
+// Spectrum bins of one gradient block: N/2 + 1 (mono r2c) or N (stereo).
+size_t conv_bins(const mufft_plan_conv *c) { return conv_stereo(c) ? c->N : c->N / 2 + 1; }
+
+bool conv_adj_spec(mufft_plan_conv *c, size_t bytes)
+{
+    if (c->adj_spec_bytes >= bytes)
+        return true;
+    cudaFree(c->adj_spec);
+    c->adj_spec = nullptr;
+    c->adj_spec_bytes = 0;
+    if (!cuda_ok(cudaMalloc(&c->adj_spec, bytes), "cudaMalloc(adjoint spectra)"))
+        return false;
+    c->adj_spec_bytes = bytes;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mufft_gb_conv_adjoint_input(mufft_plan_conv *plan, void *grad_input, const void *grad_output,
+                                const void *second_spectrum, void *stream)
+{
+    if (!plan || !grad_input || !grad_output || !second_spectrum) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    t_err = 0;
+    DeviceGuard g(plan->device);
+    const bool stereo = conv_stereo(plan);
+    const unsigned N = plan->N;
+    if (!plan->adj_fwd)
+        plan->adj_fwd = create_1d(stereo ? K_C2C : K_R2C, N, MUFFT_FORWARD, 0, 1, 0, 0, -1, false, nullptr);
+    if (!plan->adj_mul)
+        plan->adj_mul = create_1d(stereo ? K_C2C : K_C2R, N, MUFFT_INVERSE, 0, 1, 0, 0,
+                                  stereo ? PRO_MUL : PRO_MUL_C2R, false, nullptr, true);
+    if (!plan->adj_fwd || !plan->adj_mul)
+        return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+    if (!conv_adj_spec(plan, conv_bins(plan) * sizeof(float2)))
+        return t_err;
+    const cudaStream_t st = (cudaStream_t)stream;
+    int rc = exec_1d(plan->adj_fwd, plan->adj_spec, grad_output, nullptr, st, false);
+    if (rc != MUFFT_GB_OK)
+        return rc;
+    return exec_1d(plan->adj_mul, grad_input, plan->adj_spec, second_spectrum, st, false);
+}
+
+int mufft_gb_conv_adjoint_filter(mufft_plan_conv *plan, float *grad_filter, const void *grad_outputs,
+                                 size_t output_dist, const void *first_spectra, size_t spectrum_dist,
+                                 unsigned batch, void *stream)
+{
+    if (!plan || !grad_filter || !grad_outputs || !first_spectra || batch == 0) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer, or empty batch");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    t_err = 0;
+    const bool stereo = conv_stereo(plan);
+    const unsigned N = plan->N;
+    const size_t bins = conv_bins(plan);
+    if (output_dist < N || (!stereo && (output_dist & 1)) || spectrum_dist < bins) {
+        set_error(MUFFT_GB_ERR_INVALID, "batch distances smaller than one block");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (!is_device_accessible(grad_filter) || !is_device_accessible(grad_outputs) ||
+        !is_device_accessible(first_spectra)) {
+        set_error(MUFFT_GB_ERR_HOST_POINTER, "the adjoint needs device-accessible buffers");
+        return MUFFT_GB_ERR_HOST_POINTER;
+    }
+    DeviceGuard g(plan->device);
+    // Gradients are transformed in chunks whose spectra stay within 256 MiB.
+    size_t chunk = ((size_t)256 << 20) / (bins * sizeof(float2));
+    chunk = chunk < 1 ? 1 : chunk;
+    chunk = chunk > batch ? batch : chunk;
+    if (!plan->adj_fwd_batch || plan->adj_chunk != chunk || plan->adj_dist != output_dist) {
+        destroy_1d(plan->adj_fwd_batch);
+        plan->adj_fwd_batch = create_1d(stereo ? K_C2C : K_R2C, N, MUFFT_FORWARD, 0, (unsigned)chunk,
+                                        output_dist, bins, -1, false, nullptr);
+        plan->adj_chunk = plan->adj_fwd_batch ? (unsigned)chunk : 0;
+        plan->adj_dist = output_dist;
+    }
+    if (!plan->adj_c2r)
+        plan->adj_c2r = create_1d(K_C2R, N, MUFFT_INVERSE, 0, 1, 0, 0, -1, false, nullptr);
+    if (!plan->adj_fwd_batch || !plan->adj_c2r)
+        return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+    if (!conv_adj_spec(plan, chunk * bins * sizeof(float2)))
+        return t_err;
+    if (!plan->adj_acc && !cuda_ok(cudaMalloc(&plan->adj_acc, (N / 2 + 1) * sizeof(float2)), "cudaMalloc"))
+        return t_err;
+    const cudaStream_t st = (cudaStream_t)stream;
+    const size_t elem = stereo ? sizeof(float2) : sizeof(float);  // one sample of a gradient block
+    const float2 *A = (const float2 *)first_spectra;
+    for (size_t b0 = 0; b0 < batch; b0 += chunk) {
+        const size_t n = batch - b0 < chunk ? batch - b0 : chunk;
+        const char *src = (const char *)grad_outputs + b0 * output_dist * elem;
+        if (n == chunk) {
+            const int rc = exec_1d(plan->adj_fwd_batch, plan->adj_spec, src, nullptr, st, false);
+            if (rc != MUFFT_GB_OK)
+                return rc;
+        } else {
+            // ragged last chunk: one transform at a time with the single-block plan
+            if (!plan->adj_fwd)
+                plan->adj_fwd = create_1d(stereo ? K_C2C : K_R2C, N, MUFFT_FORWARD, 0, 1, 0, 0, -1, false, nullptr);
+            if (!plan->adj_fwd)
+                return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+            for (size_t i = 0; i < n; i++) {
+                const int rc = exec_1d(plan->adj_fwd, plan->adj_spec + i * bins, src + i * output_dist * elem,
+                                       nullptr, st, false);
+                if (rc != MUFFT_GB_OK)
+                    return rc;
+            }
+        }
+        if (!cuda_ok(launch_adjoint_filter_reduce(plan->adj_acc, plan->adj_spec, (long long)bins,
+                                                  A + b0 * spectrum_dist, (long long)spectrum_dist, (unsigned)n,
+                                                  N, stereo ? 1 : 0, 1.0f / (float)N, b0 > 0 ? 1 : 0, st),
+                     "adjoint reduce"))
+            return t_err;
+    }
+    return exec_1d(plan->adj_c2r, grad_filter, plan->adj_acc, nullptr, st, false);
 }
 
 }  // extern "C"

@@ -77,6 +77,7 @@ struct TileArgs {
     // convolution prologues
     const float2 *in2;        // second spectrum (B)
     float scale;
+    int conj2;                // multiply by conj(B) instead (adjoint of the convolution)
     // four-step twiddle W_N^m = exp(-2*pi*i*m/N): tw_scale = 2/N, tw_mask = N - 1;
     // for column tiles of C transforms tw_lo[k*C + c] = W_N^(k*c) (or null:
     // then every twiddle comes from sincospif)

@@ -31,7 +31,8 @@ namespace {
 
 constexpr int kThreads = 512;
 
-template <int L> __host__ __device__ constexpr int single_c() { return kThreads * 16 / L; }
+template <int L> __host__ __device__ constexpr int single_r() { return L > 8192 ? 32 : 16; }
+template <int L> __host__ __device__ constexpr int single_c() { return kThreads * single_r<L>() / L; }
 
 // Forward tile into the spectrum scratch, then the fused multiply + inverse
 // tile into the output.
@@ -39,7 +40,7 @@ template <int L>
 __device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
                             const float2 *rtw_inv)
 {
-    constexpr int C = single_c<L>();
+    constexpr int C = single_c<L>(), R = single_r<L>();
     const bool mono = q.stereo == 0;
     TileArgs f{};
     f.in = q.in;
@@ -52,7 +53,7 @@ __device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, 
     f.tw = tw;
     f.rtw = rtw_fwd;
     f.scale = 1.0f;
-    tile_body<L, 16, C, 1, ALONG, ALONG, false>(f, 0, 0, 0, 0, smem);
+    tile_body<L, R, C, 1, ALONG, ALONG, false>(f, 0, 0, 0, 0, smem);
     __syncthreads();  // spectrum complete and visible to the whole CTA
 
     TileArgs b{};
@@ -68,7 +69,7 @@ __device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, 
     b.scale = q.scale;
     b.conj = 3;
     b.tw = tw;
-    tile_body<L, 16, C, 1, ALONG, ALONG, true>(b, 0, 0, 0, 0, smem);
+    tile_body<L, R, C, 1, ALONG, ALONG, true>(b, 0, 0, 0, 0, smem);
     __syncthreads();
 }
 
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedAr
         case 11: conv_single<2048>(q, smem, args.tw, rf, ri); break;
         case 12: conv_single<4096>(q, smem, args.tw, rf, ri); break;
         case 13: conv_single<8192>(q, smem, args.tw, rf, ri); break;
-        case 14: conv_multi<128, 128>(q, smem, args.tw, rf, ri); break;
+        case 14: conv_single<16384>(q, smem, args.tw, rf, ri); break;
         case 15: conv_multi<128, 256>(q, smem, args.tw, rf, ri); break;
         case 16: conv_multi<256, 256>(q, smem, args.tw, rf, ri); break;
         default: break;
@@ -203,7 +204,10 @@ __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedAr
     }
 }
 
-template <int L> constexpr size_t single_bytes() { return tile_exchange_bytes<L, 16, single_c<L>(), 1, ALONG, ALONG>(); }
+template <int L> constexpr size_t single_bytes()
+{
+    return tile_exchange_bytes<L, single_r<L>(), single_c<L>(), 1, ALONG, ALONG>();
+}
 template <int L1, int L2> constexpr size_t multi_bytes()
 {
     constexpr size_t a = tile_exchange_bytes<L1, 16, kThreads * 16 / L1, 1, ACROSS, ACROSS>();
@@ -216,7 +220,7 @@ size_t conv_ragged_smem()
     // every tile conv_ragged_kernel instantiates
     const size_t v[] = {single_bytes<16>(),   single_bytes<32>(),   single_bytes<64>(),   single_bytes<128>(),
                         single_bytes<256>(),  single_bytes<512>(),  single_bytes<1024>(), single_bytes<2048>(),
-                        single_bytes<4096>(), single_bytes<8192>(), multi_bytes<128, 128>(),
+                        single_bytes<4096>(), single_bytes<8192>(), single_bytes<16384>(),
                         multi_bytes<128, 256>(), multi_bytes<256, 256>()};
     size_t m = 0;
     for (size_t x : v)

@@ -394,7 +394,9 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
             for (int m = 0; m < r; m++)
                 if (m < mlim) {
                     const long long o = (long long)(TL * u + m * Q * B) * sst;
-                    v[u * r + m] = cscale(cmul(gload<COH>(f + o), gload<COH>(g + o)), a.scale);
+                    float2 gv = gload<COH>(g + o);
+                    gv.y = a.conj2 ? -gv.y : gv.y;
+                    v[u * r + m] = cscale(cmul(gload<COH>(f + o), gv), a.scale);
                 }
         break;
     }
@@ -412,8 +414,13 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
                     const long long ia = tb + local, ib = tb + a.mirror_len - local;
                     float2 xa = gload<COH>(&in[ia]), xb = gload<COH>(&in[ib]);
                     if (mul) {
-                        xa = cscale(cmul(xa, gload<COH>(&in2[ia])), a.scale);
-                        xb = cscale(cmul(xb, gload<COH>(&in2[ib])), a.scale);
+                        float2 ga = gload<COH>(&in2[ia]), gb = gload<COH>(&in2[ib]);
+                        if (a.conj2) {
+                            ga.y = -ga.y;
+                            gb.y = -gb.y;
+                        }
+                        xa = cscale(cmul(xa, ga), a.scale);
+                        xb = cscale(cmul(xb, gb), a.scale);
                     }
                     v[u * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
                 }

@@ -48,6 +48,43 @@ __global__ void spectral_multiply(float2 *out, const float2 *__restrict__ a, con
         out[i] = cscale(cmul(a[i], b[i]), s);
 }
 
+// Filter adjoint, frequency-domain reduction over a chunk of signals, for
+// bins k = 0 .. N/2 of the real filter's gradient spectrum:
+//   mono (r2c spectra, k <= N/2):  acc[k] (+)= s * sum_i G_i[k] conj(A_i[k])
+//   stereo (full c2c spectra):     acc[k] (+)= s/2 * sum_i (G_i[k] conj(A_i[k])
+//                                               + conj(G_i[N-k] conj(A_i[N-k])))
+// The stereo form is the Hermitian part of the correlation spectrum, whose
+// c2r inverse is the real part of the complex correlation.  Signals are
+// summed in index order (deterministic).
+__global__ void adjoint_filter_reduce(float2 *acc, const float2 *__restrict__ g, long long gdist,
+                                      const float2 *__restrict__ a, long long adist, unsigned count,
+                                      unsigned N, int stereo, float s, int accumulate)
+{
+    const unsigned nb = N / 2 + 1;
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += gridDim.x * blockDim.x) {
+        const unsigned km = (N - k) & (N - 1);
+        float2 sum = make_float2(0.f, 0.f);
+        for (unsigned i = 0; i < count; i++) {
+            const float2 *gi = g + (long long)i * gdist, *ai = a + (long long)i * adist;
+            const float2 gk = gi[k], ak = ai[k];
+            sum.x += gk.x * ak.x + gk.y * ak.y;  // G conj(A)
+            sum.y += gk.y * ak.x - gk.x * ak.y;
+            if (stereo) {
+                const float2 gm = gi[km], am = ai[km];
+                sum.x += gm.x * am.x + gm.y * am.y;  // conj(G conj(A)) at N-k
+                sum.y -= gm.y * am.x - gm.x * am.y;
+            }
+        }
+        const float f = stereo ? 0.5f * s : s;
+        float2 r = make_float2(sum.x * f, sum.y * f);
+        if (accumulate) {
+            r.x += acc[k].x;
+            r.y += acc[k].y;
+        }
+        acc[k] = r;
+    }
+}
+
 __global__ void fill_u32(unsigned *p, unsigned v, unsigned long long n)
 {
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
@@ -75,6 +112,18 @@ cudaError_t launch_spectral_multiply(float2 *out, const float2 *a, const float2 
     if (blocks > 8192)
         blocks = 8192;
     spectral_multiply<<<(unsigned)blocks, 256, 0, st>>>(out, a, b, s, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_filter_reduce(float2 *acc, const float2 *g, long long gdist, const float2 *a,
+                                         long long adist, unsigned count, unsigned N, int stereo, float s,
+                                         int accumulate, cudaStream_t st)
+{
+    const unsigned nb = N / 2 + 1;
+    unsigned blocks = (nb + 255) / 256;
+    if (blocks > 8192)
+        blocks = 8192;
+    adjoint_filter_reduce<<<blocks, 256, 0, st>>>(acc, g, gdist, a, adist, count, N, stereo, s, accumulate);
     return cudaGetLastError();
 }
 

@@ -9,6 +9,9 @@ cudaError_t launch_r2c_fixup_inplace(float2 *z, const float2 *rtw, long long M, 
                                      unsigned batch, int full, cudaStream_t st);
 cudaError_t launch_spectral_multiply(float2 *out, const float2 *a, const float2 *b, float s,
                                      unsigned long long n, cudaStream_t st);
+cudaError_t launch_adjoint_filter_reduce(float2 *acc, const float2 *g, long long gdist, const float2 *a,
+                                         long long adist, unsigned count, unsigned N, int stereo, float s,
+                                         int accumulate, cudaStream_t st);
 cudaError_t launch_fill_u32(unsigned *p, unsigned v, unsigned long long n, cudaStream_t st);
 
 }  // namespace mgb

@@ -1,0 +1,195 @@
+"""GPU tests of the convolution adjoints (mufft_gb_conv_adjoint_input /
+_filter) against the FP64 oracle (oracle/adjoint.py), finite differences of
+the loss, and a 200-step gradient descent that recovers a hidden filter."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+from mufft_gb300 import capi as K
+from mufft_gb300 import signals
+from oracle import adjoint as A
+
+pytestmark = pytest.mark.gpu
+
+STEREO = K.CONV_METHOD_FLAG_STEREO_MONO
+PAD1 = K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST
+PAD2 = K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND
+ADJ_TOL = 1e-5  # relative L2 against FP64 (the bar for gradients is 1e-4)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import mufft_gb300
+    return mufft_gb300.load()
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available()
+    return t
+
+
+def _st(torch):
+    return torch.cuda.current_stream().cuda_stream
+
+
+class ConvPlan:
+    def __init__(self, gpu, N, method):
+        self.gpu, self.N, self.method = gpu, N, method
+        self.stereo = bool(method & 1)
+        self.p = gpu.create_plan_conv(N, 0, method)
+        assert self.p, gpu.gb_last_error_string()
+        self.block = gpu.conv_get_transformed_block_size(self.p) // 8
+
+    def spectrum(self, torch, block, x_dev):
+        out = torch.empty(self.block, dtype=torch.complex64, device="cuda")
+        rc = self.gpu.gb_execute_conv_input_async(self.p, block, out.data_ptr(), x_dev.data_ptr(), _st(torch))
+        assert rc == 0, self.gpu.gb_last_error_string()
+        return out
+
+    def free(self):
+        self.gpu.free_plan_conv(self.p)
+
+
+def _signal(seed, N, stereo):
+    return signals.complex_uniform(seed, N) if stereo else signals.uniform(seed, N)
+
+
+def _dev(torch, x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+@pytest.mark.parametrize("N", [16, 256, 4096, 1 << 16, 1 << 21])
+@pytest.mark.parametrize("method", [0, STEREO, PAD1 | PAD2, STEREO | PAD2])
+def test_adjoint_input_vs_fp64(gpu, torch, N, method):
+    pl = ConvPlan(gpu, N, method)
+    try:
+        b = signals.uniform(30000 + N, N)
+        g = _signal(30001 + N, N, pl.stereo)
+        H = pl.spectrum(torch, K.CONV_BLOCK_SECOND, _dev(torch, b))
+        dg = _dev(torch, g)
+        out = torch.full((N,), float("nan"), dtype=torch.complex64 if pl.stereo else torch.float32, device="cuda")
+        rc = gpu.gb_conv_adjoint_input(pl.p, out.data_ptr(), dg.data_ptr(), H.data_ptr(), _st(torch))
+        assert rc == 0, gpu.gb_last_error_string()
+        torch.cuda.synchronize()
+    finally:
+        pl.free()
+    b_eff = b.astype(np.float64)
+    if method & PAD2:
+        b_eff[N // 2:] = 0
+    ref = A.adjoint_input_f64(g, b_eff, pl.stereo)
+    assert rel_l2(out.cpu().numpy(), ref) < ADJ_TOL
+
+
+@pytest.mark.parametrize("N,B", [(16, 1), (1024, 7), (1 << 16, 3), (1 << 21, 2), (1 << 23, 5)])
+@pytest.mark.parametrize("method", [0, STEREO | PAD1])
+def test_adjoint_filter_vs_fp64(gpu, torch, N, B, method):
+    """Batch sums over spectra; (2^23, 5) runs a ragged last chunk."""
+    if N == 1 << 23 and not method & 1:
+        pytest.skip("the ragged chunk needs the stereo spectrum size")
+    pl = ConvPlan(gpu, N, method)
+    try:
+        firsts = np.stack([_signal(31000 + N + i, N, pl.stereo) for i in range(B)])
+        grads = np.stack([_signal(32000 + N + i, N, pl.stereo) for i in range(B)])
+        dA = torch.empty((B, pl.block), dtype=torch.complex64, device="cuda")
+        for i in range(B):
+            dA[i] = pl.spectrum(torch, K.CONV_BLOCK_FIRST, _dev(torch, firsts[i]))
+        dg = _dev(torch, grads)
+        out = torch.full((N,), float("nan"), dtype=torch.float32, device="cuda")
+        rc = gpu.gb_conv_adjoint_filter(pl.p, out.data_ptr(), dg.data_ptr(), N, dA.data_ptr(), pl.block, B,
+                                        _st(torch))
+        assert rc == 0, gpu.gb_last_error_string()
+        torch.cuda.synchronize()
+    finally:
+        pl.free()
+    f_eff = firsts.astype(np.complex128 if pl.stereo else np.float64)
+    if method & PAD1:
+        f_eff[:, N // 2:] = 0
+    ref = A.adjoint_filter_f64(grads, f_eff)
+    assert rel_l2(out.cpu().numpy(), ref) < ADJ_TOL
+
+
+@pytest.mark.parametrize("method", [0, STEREO])
+def test_adjoint_matches_finite_differences(gpu, torch, method):
+    """GPU gradients of 0.5*||conv(first, second) - target||^2 against FP64
+    central differences, to 1e-4 relative."""
+    N, B = 128, 2
+    pl = ConvPlan(gpu, N, method)
+    try:
+        firsts = np.stack([_signal(33000 + i, N, pl.stereo) for i in range(B)])
+        second = signals.uniform(33100, N)
+        targets = np.stack([_signal(33200 + i, N, pl.stereo) for i in range(B)])
+        r = np.stack([A.conv_f64(f, second, pl.stereo) for f in firsts]) - targets
+        r32 = r.astype(np.complex64 if pl.stereo else np.float32)
+        H = pl.spectrum(torch, K.CONV_BLOCK_SECOND, _dev(torch, second))
+        dA = torch.stack([pl.spectrum(torch, K.CONV_BLOCK_FIRST, _dev(torch, f)) for f in firsts])
+        dr = _dev(torch, r32)
+        gf = torch.empty(N, dtype=torch.float32, device="cuda")
+        assert gpu.gb_conv_adjoint_filter(pl.p, gf.data_ptr(), dr.data_ptr(), N, dA.data_ptr(), pl.block, B,
+                                          _st(torch)) == 0
+        gi = torch.empty(N, dtype=torch.complex64 if pl.stereo else torch.float32, device="cuda")
+        assert gpu.gb_conv_adjoint_input(pl.p, gi.data_ptr(), dr[1].data_ptr(), H.data_ptr(), _st(torch)) == 0
+        torch.cuda.synchronize()
+    finally:
+        pl.free()
+    gf, gi = gf.cpu().numpy(), gi.cpu().numpy()
+    scale_f, scale_i = np.abs(gf).max(), np.abs(gi).max()
+    for j in (0, 3, 64, N - 1):
+        fd = A.finite_difference(lambda s: A.loss_f64(firsts, s, targets, pl.stereo), second.astype(np.float64), j)
+        assert abs(fd - gf[j]) < 1e-4 * scale_f, ("filter", j, fd, gf[j])
+
+        def loss_first(f1):
+            f = firsts.astype(f1.dtype)
+            f[1] = f1
+            return A.loss_f64(f, second, targets, pl.stereo)
+        x1 = firsts[1].astype(np.complex128 if pl.stereo else np.float64)
+        fd = A.finite_difference(loss_first, x1, j)
+        assert abs(fd - gi[j]) < 1e-4 * scale_i, ("input", j, fd, gi[j])
+
+
+def test_gradient_descent_recovers_filter(gpu, torch):
+    """200 steps of gradient descent on the taps of a filter shared by 8 stereo
+    signals (conv_input, conv_output and the filter adjoint on the GPU)."""
+    N, B, T = 4096, 8, 128
+    method = STEREO | PAD1 | PAD2
+    t = np.arange(T)
+    h_true = signals.normal(34000, T) * np.exp(-t / (T / 4))
+    x = np.zeros((B, N), np.complex64)
+    for i in range(B):
+        x[i, : N // 2] = signals.complex_uniform(34100 + i, N // 2)
+    h_pad = np.zeros(N)
+    h_pad[:T] = h_true
+    targets = np.stack([A.conv_f64(x[i], h_pad, True) for i in range(B)]).astype(np.complex64)
+    spec = np.fft.fft(x.astype(np.complex128), axis=1)
+    lr = 1.0 / float(np.max(np.sum(np.abs(spec) ** 2, axis=0)))
+
+    pl = ConvPlan(gpu, N, method)
+    try:
+        dA = torch.stack([pl.spectrum(torch, K.CONV_BLOCK_FIRST, _dev(torch, x[i])) for i in range(B)])
+        dt = _dev(torch, targets)
+        h = torch.zeros(N, dtype=torch.float32, device="cuda")
+        y = torch.empty((B, N), dtype=torch.complex64, device="cuda")
+        grad = torch.empty(N, dtype=torch.float32, device="cuda")
+        st = _st(torch)
+        losses = []
+        for step in range(200):
+            H = pl.spectrum(torch, K.CONV_BLOCK_SECOND, h)
+            for i in range(B):
+                assert gpu.gb_execute_conv_output_async(pl.p, y[i].data_ptr(), dA[i].data_ptr(), H.data_ptr(),
+                                                        st) == 0
+            r = y - dt
+            losses.append(0.5 * float(torch.sum(torch.abs(r) ** 2)))
+            assert gpu.gb_conv_adjoint_filter(pl.p, grad.data_ptr(), r.data_ptr(), N, dA.data_ptr(), pl.block,
+                                              B, st) == 0
+            h[:T] -= lr * grad[:T]
+        h_got = h[:T].cpu().numpy()
+    finally:
+        pl.free()
+    assert losses[-1] < 1e-8 * losses[0], (losses[0], losses[-1])
+    # monotone until the FP32 floor
+    far = [i for i in range(1, len(losses)) if losses[i - 1] > 1e-6 * losses[0]]
+    assert len(far) >= 5 and all(losses[i] <= losses[i - 1] for i in far), losses[:12]
+    assert rel_l2(h_got, h_true) < 1e-4
