@@ -30,6 +30,15 @@ extern "C" {
 #define MUFFT_GB_ERR_HOST_POINTER (-4)/* async call given host memory */
 #define MUFFT_GB_ERR_ALLOC (-5)
 
+/* Extension plan flags (bits the reference leaves unused, fft.h:52-65).
+ * Split precision: c2c transforms of N = 256 or 4096 whose radix-16 stages
+ * run as 16x16 DFT-matrix products on the tensor cores, with FP32 values
+ * carried as BF16 limbs and FP32 accumulation.  No reference counterpart.
+ *   BF16X3: three limbs, six products -- FP32-level error.
+ *   BF16X2: two limbs, three products -- about 1e-5 relative error. */
+#define MUFFT_GB_FLAG_SPLIT_BF16X3 (1u << 24)
+#define MUFFT_GB_FLAG_SPLIT_BF16X2 (1u << 25)
+
 /* Last error of the calling thread (0 if none) and its text. */
 int mufft_gb_last_error(void);
 const char *mufft_gb_last_error_string(void);

@@ -24,6 +24,9 @@ FLAG_CPU_NO_SSE3 = 1 << 1
 FLAG_CPU_NO_SSE = 1 << 2
 FLAG_FULL_R2C = 1 << 16
 FLAG_ZERO_PAD_UPPER_HALF = 1 << 17
+# mufft_gb300.h extension flags
+FLAG_SPLIT_BF16X3 = 1 << 24
+FLAG_SPLIT_BF16X2 = 1 << 25
 CONV_METHOD_FLAG_MONO_MONO = 0
 CONV_METHOD_FLAG_STEREO_MONO = 1
 CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST = 1 << 2

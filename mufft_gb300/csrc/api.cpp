@@ -32,6 +32,7 @@
 #include "common.h"
 #include "conv_ragged.h"
 #include "misc_kernels.h"
+#include "split_tc.h"
 #include "registry.h"
 
 using namespace mgb;
@@ -258,7 +259,7 @@ bool is_device_accessible(const void *p)
 // ================================================================ passes
 
 enum Role { ROLE_NONE = 0, ROLE_IN, ROLE_OUT, ROLE_IN2, ROLE_SCRATCH };
-enum PassType { PASS_TILE = 0, PASS_R2C_FIXUP = 1, PASS_BC = 2 };
+enum PassType { PASS_TILE = 0, PASS_R2C_FIXUP = 1, PASS_BC = 2, PASS_SPLIT = 3 };
 
 struct Pass {
     PassType type = PASS_TILE;
@@ -274,6 +275,10 @@ struct Pass {
     BcArgs bc{};
     size_t bc_counter_bytes = 0;
     unsigned bc_grid = 0;
+    // split-precision tensor-core transform (split_tc.cu)
+    SplitArgs sp{};
+    int sp_stages = 0, sp_limbs = 0;
+    unsigned sp_grid = 0;
 };
 
 struct Buffers {
@@ -329,6 +334,15 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             }
             if (e != cudaSuccess)
                 return e;
+        } else if (p.type == PASS_SPLIT) {
+            SplitArgs a = p.sp;
+            a.in = (const float2 *)pick(p.in_role, b);
+            a.out = (float2 *)pick(p.out_role, b);
+            void *args[] = {&a};
+            cudaError_t e = cudaLaunchKernel(split_kernel(p.sp_stages, p.sp_limbs), dim3(p.sp_grid),
+                                             dim3(kSplitThreads), args, split_smem_bytes(), st);
+            if (e != cudaSuccess)
+                return e;
         } else if (p.type == PASS_BC) {
             BcArgs a = p.bc;
             a.y = (const float2 *)b.scratch;
@@ -372,6 +386,9 @@ std::string describe(const std::vector<Pass> &ps)
                      i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue), p.a.conj);
+        else if (p.type == PASS_SPLIT)
+            snprintf(buf, sizeof(buf), "%ssplit_tc N=%d bf16x%d grid=%u threads=%d smem=%zu conj=%d", i ? "; " : "",
+                     1 << (4 * p.sp_stages), p.sp_limbs, p.sp_grid, kSplitThreads, split_smem_bytes(), p.sp.conj);
         else if (p.type == PASS_BC)
             snprintf(buf, sizeof(buf), "%sfused_bc 256x256 rows=%u blocks=%u ring=%u grid=%u", i ? "; " : "",
                      p.bc.n1, p.bc.nblk, p.bc.ring_slots, p.bc_grid);
@@ -406,8 +423,14 @@ struct PlanResources {
     float2 *ring = nullptr;       // fused B/C: L2-resident ring of row blocks
     unsigned *counters = nullptr; // fused B/C: task counters
     int *err = nullptr;           // device error flag of bounded waits
+    unsigned *afrag = nullptr;    // split precision: DFT-16 limbs in mma fragment order
+    float2 *sptw = nullptr;       // split precision: stage twiddles
     void release()
     {
+        cudaFree(afrag);
+        cudaFree(sptw);
+        afrag = nullptr;
+        sptw = nullptr;
         cudaFree(rtw);
         cudaFree(twlo);
         cudaFree(twlo2);
@@ -882,6 +905,13 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
     }
     const bool zp = (flags & MUFFT_FLAG_ZERO_PAD_UPPER_HALF) != 0;
     const bool full = (flags & MUFFT_FLAG_FULL_R2C) != 0;
+    const int split_limbs =
+        (flags & MUFFT_GB_FLAG_SPLIT_BF16X3) ? 3 : ((flags & MUFFT_GB_FLAG_SPLIT_BF16X2) ? 2 : 0);
+    if (split_limbs && (kind != K_C2C || (N != 256 && N != 4096) || zp || prologue_override >= 0)) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED,
+                  "split-precision transforms are c2c of N = 256 or 4096 without zero padding");
+        return nullptr;
+    }
 
     mufft_plan_1d *pl = new mufft_plan_1d();
     pl->kind = kind;
@@ -967,7 +997,34 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
         s.scale = 1.0f / (float)N;
     if (prologue_override >= 0 && kind == K_C2R)
         s.scale = 1.0f / (float)N;
-    if (!build_fft_passes(s, tw, pl->res, dry, pl->passes)) {
+    if (split_limbs) {
+        Pass p;
+        p.type = PASS_SPLIT;
+        p.sp.in_dist = s.in_dist;
+        p.sp.out_dist = s.out_dist;
+        p.sp.ntrans = batch;
+        p.sp.conj = direction == MUFFT_INVERSE ? 1 : 0;
+        p.sp_stages = N == 256 ? 2 : 3;
+        p.sp_limbs = split_limbs;
+        const unsigned per_cta = kSplitPoints / N;
+        p.sp_grid = (batch + per_cta - 1) / per_cta;
+        if (!dry) {
+            const std::vector<unsigned> af = split_afrag_table();
+            if (!cuda_ok(cudaMalloc(&pl->res.afrag, af.size() * sizeof(unsigned)), "cudaMalloc(split table)") ||
+                !cuda_ok(cudaMemcpy(pl->res.afrag, af.data(), af.size() * sizeof(unsigned), cudaMemcpyHostToDevice),
+                         "cudaMemcpy(split table)") ||
+                !(pl->res.sptw = upload(split_twiddle_table())) ||
+                !cuda_ok(cudaFuncSetAttribute(split_kernel(p.sp_stages, split_limbs),
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_smem_bytes()),
+                         "cudaFuncSetAttribute(split)")) {
+                destroy_1d(pl);
+                return nullptr;
+            }
+            p.sp.afrag = pl->res.afrag;
+            p.sp.tw = pl->res.sptw;
+        }
+        pl->passes.push_back(p);
+    } else if (!build_fft_passes(s, tw, pl->res, dry, pl->passes)) {
         destroy_1d(pl);
         return nullptr;
     }

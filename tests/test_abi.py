@@ -71,6 +71,29 @@ def test_constants_match_reference():
         assert m and m.group(1).strip() == v, k
 
 
+def test_extension_flags_match_header():
+    h = (ROOT / "include" / "mufft_gb300.h").read_text()
+    for name, val in (("MUFFT_GB_FLAG_SPLIT_BF16X3", K.FLAG_SPLIT_BF16X3),
+                      ("MUFFT_GB_FLAG_SPLIT_BF16X2", K.FLAG_SPLIT_BF16X2)):
+        m = re.search(rf"#define {name}\s+\(1u << (\d+)\)", h)
+        assert m and (1 << int(m.group(1))) == val, name
+    # no overlap with the reference's flag bits (fft.h:52-65)
+    assert K.FLAG_SPLIT_BF16X3 & (K.FLAG_CPU_NO_SIMD | K.FLAG_FULL_R2C | K.FLAG_ZERO_PAD_UPPER_HALF) == 0
+
+
+def test_split_precision_schedule_and_rejections(lib):
+    buf = C.create_string_buffer(4096)
+    for N, limbs, flag in ((4096, 3, K.FLAG_SPLIT_BF16X3), (256, 2, K.FLAG_SPLIT_BF16X2)):
+        assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, buf, 4096) == 0
+        d = buf.value.decode()
+        assert d.startswith(f"split_tc N={N} bf16x{limbs}"), d
+        assert f"grid={65536 * N // 4096}" in d, d
+    for N, kind, flags in ((1024, 0, K.FLAG_SPLIT_BF16X3), (4096, 1, K.FLAG_SPLIT_BF16X3),
+                           (4096, 0, K.FLAG_SPLIT_BF16X2 | K.FLAG_ZERO_PAD_UPPER_HALF)):
+        assert lib.gb_describe_schedule_1d(N, kind, K.FORWARD, flags, 1, buf, 4096) == -2, (N, kind, flags)
+        lib.gb_clear_error()
+
+
 def test_null_frees_are_noops(lib):
     lib.free_plan_1d(None)
     lib.free_plan_2d(None)
