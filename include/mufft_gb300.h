@@ -196,9 +196,11 @@ int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsi
  * 2 (four-step) or 3 (three-level decomposition with smaller tiles); 0
  * restores the automatic choice.  Affects plans created afterwards. */
 int mufft_gb_set_multipass_levels(unsigned levels);
-/* Inter-pass twiddles of multi-pass transforms from a per-plan FP64 table
- * (1) or from sincospif (0); -1 restores the automatic choice by tile length.
- * Affects plans created afterwards. */
+/* Inter-pass twiddles of multi-pass transforms: from sincospif per element
+ * (0), from a per-plan FP64 table times a per-tile factor (1), or from
+ * per-tile column powers times one factor per thread (2); -1 restores the
+ * automatic choice (2 where the column tile has room, else 0).  Affects plans
+ * created afterwards. */
 int mufft_gb_set_twiddle_table(int mode);
 /* Three-level transforms of N1 x 65536 points run their last two passes as one
  * persistent launch whose intermediate stays in L2 (enable = 1) or as two

@@ -312,7 +312,7 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             a.out = (float2 *)pick(p.out_role, b);
             a.in2 = (const float2 *)pick(p.in2_role, b);
             void *args[] = {&a};
-            const size_t smem = a.tw_lo ? p.k->smem : p.k->smem_ex;
+            const size_t smem = (a.tw_lo || a.tw_colpow) ? p.k->smem : p.k->smem_ex;
             cudaError_t e;
             if (p.k->Q > 1) {
                 // one tile per cluster of Q CTAs (distributed shared memory)
@@ -382,10 +382,12 @@ std::string describe(const std::vector<Pass> &ps)
     for (size_t i = 0; i < ps.size(); i++) {
         const Pass &p = ps[i];
         if (p.type == PASS_TILE)
-            snprintf(buf, sizeof(buf), "%stile L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s conj=%d",
+            snprintf(buf, sizeof(buf), "%stile L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s%s conj=%d",
                      i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
-                     pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue), p.a.conj);
+                     pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
+                     p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
+                     p.a.conj);
         else if (p.type == PASS_SPLIT)
             snprintf(buf, sizeof(buf), "%ssplit_tc N=%d bf16x%d grid=%u threads=%d smem=%zu conj=%d", i ? "; " : "",
                      1 << (4 * p.sp_stages), p.sp_limbs, p.sp_grid, kSplitThreads, split_smem_bytes(), p.sp.conj);
@@ -447,10 +449,11 @@ struct PlanResources {
 // Multi-pass depth for transforms longer than one tile: 0 = automatic
 // (set with mufft_gb_set_multipass_levels).
 std::atomic<int> g_levels{0};
-// Four-step twiddles of column passes from the per-plan table (1), from
-// sincospif (0), or by tile length (-1: table for L <= 512, where the extra
-// shared memory costs no occupancy; longer tiles are bound by load/store
-// issue, which sincospif on the otherwise idle XU pipe avoids).
+// Four-step twiddles of column passes: sincospif per element (0), the
+// per-plan table times a per-tile factor (1), or per-tile column powers (2).
+// Automatic (-1): column powers wherever the tile has the shared-memory
+// region -- one sincospif per thread plus shared-memory reads, no per-element
+// global table loads on the load/store path.
 std::atomic<int> g_twiddle_table{-1};
 // Fuse the last two passes of M = N1 x 65536 transforms into one persistent
 // launch with an L2-resident intermediate (1), or run them separately (0,
@@ -461,7 +464,16 @@ std::atomic<int> g_fused_bc{0};
 bool use_twiddle_table(const TileKernel *k)
 {
     const int t = g_twiddle_table.load();
-    return k->has_thi && (t == 1 || (t < 0 && k->L <= 512));
+    return k->has_thi && t == 1;
+}
+
+// Column powers (mode 2, and the automatic choice wherever the tile has the
+// shared-memory region): the twiddles of a column are W^(col*base) of each
+// thread times R per-column powers computed once per tile.
+bool use_colpow(const TileKernel *k)
+{
+    const int t = g_twiddle_table.load();
+    return k->has_thi && (t == 2 || t < 0);
 }
 
 // W_M^(k*c) for k < L, c < C: the per-column half of a four-step twiddle.
@@ -492,6 +504,7 @@ Pass column_pass(const TileKernel *k, const float2 *tw, unsigned L, unsigned nco
     p.a.tw_scale = 2.0f / (float)Mtw;
     p.a.tw_mask = (unsigned)(Mtw - 1);
     p.a.tw_lo = use_twiddle_table(k) ? twlo : nullptr;
+    p.a.tw_colpow = use_colpow(k) ? 1 : 0;
     p.a.scale = 1.0f;
     (void)L;
     return p;
@@ -772,6 +785,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p1.a.tw_scale = 2.0f / (float)M;
     p1.a.tw_mask = M - 1;
     p1.a.tw_lo = use_twiddle_table(kc) ? res.twlo : nullptr;
+    p1.a.tw_colpow = use_colpow(kc) ? 1 : 0;
     p1.in_role = s.in_role;
     p1.in2_role = s.in2_role;
     p1.a.conj2 = s.conj2;
@@ -1982,8 +1996,8 @@ int mufft_gb_device_synchronize(void)
 
 int mufft_gb_set_twiddle_table(int mode)
 {
-    if (mode < -1 || mode > 1) {
-        set_error(MUFFT_GB_ERR_INVALID, "mode must be -1 (automatic), 0 or 1");
+    if (mode < -1 || mode > 2) {
+        set_error(MUFFT_GB_ERR_INVALID, "mode must be -1 (automatic), 0, 1 or 2");
         return MUFFT_GB_ERR_INVALID;
     }
     g_twiddle_table.store(mode);

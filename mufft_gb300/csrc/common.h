@@ -84,6 +84,9 @@ struct TileArgs {
     float tw_scale;
     unsigned tw_mask;
     const float2 *tw_lo;
+    // nonzero: per-tile column powers instead (W_N^(col*off) for the R output
+    // offsets of each column in shared memory, times W_N^(col*base) per thread)
+    int tw_colpow;
 };
 
 }  // namespace mgb

@@ -473,20 +473,30 @@ __host__ __device__ constexpr size_t tile_exchange_bytes()
 
 constexpr size_t kMaxSmemPerCta = 227 * 1024;
 
-// ... and, for single-CTA column passes where it fits, the per-tile half of
-// the four-step twiddle (L values); without it the twiddles come from sincospif.
+// ... and, for single-CTA column passes where it fits, a four-step twiddle
+// region: the per-tile half W_N^(k*C*tile) of every output k (L values, with
+// the plan's table tw_lo), or the column powers W_N^(col*off) of the R output
+// offsets of each of the C columns (tw_colpow); without it the twiddles come
+// from sincospif.
+template <int L, int R, int C, int Q, int LMAP, int SMAP>
+__host__ __device__ constexpr size_t tile_twr_elems()
+{
+    return (size_t)L > (size_t)C * R ? (size_t)L : (size_t)C * R;
+}
+
 template <int L, int R, int C, int Q, int LMAP, int SMAP>
 __host__ __device__ constexpr bool tile_has_thi()
 {
     return Q == 1 && LMAP == ACROSS && SMAP == ACROSS &&
-           tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() + (size_t)L * sizeof(float2) <= kMaxSmemPerCta;
+           tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() + tile_twr_elems<L, R, C, Q, LMAP, SMAP>() * sizeof(float2) <=
+               kMaxSmemPerCta;
 }
 
 template <int L, int R, int C, int Q, int LMAP, int SMAP>
 __host__ __device__ constexpr size_t tile_smem_bytes()
 {
     return tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() +
-           (tile_has_thi<L, R, C, Q, LMAP, SMAP>() ? (size_t)L * sizeof(float2) : 0);
+           (tile_has_thi<L, R, C, Q, LMAP, SMAP>() ? tile_twr_elems<L, R, C, Q, LMAP, SMAP>() * sizeof(float2) : 0);
 }
 
 
@@ -541,10 +551,21 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
 
     static_assert(tile_smem_bytes<L, R, C, Q, LMAP, SMAP>() <= kMaxSmemPerCta, "tile exceeds shared memory");
     if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
-        // Four-step twiddle, per-tile half: W_N^(k*C*tile) for every output k
-        // (the per-column half W_N^(k*c) comes from the plan's table tw_lo).
-        if (a.epilogue == EPI_TWIDDLE && a.tw_lo) {
-            float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
+        float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
+        if (a.epilogue == EPI_TWIDDLE && a.tw_colpow) {
+            // W_N^(col*off_i), col = tile*C + c, for the last stage's output
+            // offsets off_i = TL*u + m*BL of register i = u*rl + m
+            constexpr int rl = S::radix(NST - 1), BL = TT::B(NST - 1);
+            for (int idx = threadIdx.x; idx < C * R; idx += tile_threads<L, R, C, Q>()) {
+                const int cc = idx % C, i = idx / C;  // [i][c]: neighbouring columns in neighbouring banks
+                const unsigned off = (unsigned)(TL * (i / rl) + (i % rl) * BL);
+                thi[idx] = fourstep_twiddle((tile0 + cc) * off, a.tw_scale, a.tw_mask);
+            }
+            if constexpr (NST == 1)
+                __syncthreads();
+        } else if (a.epilogue == EPI_TWIDDLE && a.tw_lo) {
+            // Four-step twiddle, per-tile half: W_N^(k*C*tile) for every output k
+            // (the per-column half W_N^(k*c) comes from the plan's table tw_lo).
             for (int k = threadIdx.x; k < L; k += tile_threads<L, R, C, Q>())
                 thi[k] = fourstep_twiddle((unsigned)k * (unsigned)(C * tile), a.tw_scale, a.tw_mask);
             if constexpr (NST == 1)
@@ -636,8 +657,13 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         float2 *o0 = out + obase + (long long)p0 * sst;
         if (a.epilogue == EPI_TWIDDLE) {
             // W_N^(k*n) for output k of column n = tile*C + c.
-            // W_N^(k*C*tile), filled at kernel start, after the exchange slices
+            // Twiddle region (filled at kernel start, after the exchange slices)
             float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
+            float2 wbase = make_float2(1.f, 0.f);
+            if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
+                if (a.tw_colpow)
+                    wbase = fourstep_twiddle((unsigned)p0 * tr, a.tw_scale, a.tw_mask);
+            }
 #pragma unroll
             for (int u = 0; u < NBL; u++)
 #pragma unroll
@@ -646,7 +672,9 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     const int k = p0 + off;
                     float2 w;
                     if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
-                        if (a.tw_lo)
+                        if (a.tw_colpow)
+                            w = cmul(wbase, thi[(u * rl + m) * C + c]);
+                        else if (a.tw_lo)
                             w = cmul(__ldg(&a.tw_lo[k * C + c]), thi[k]);
                         else
                             w = fourstep_twiddle((unsigned)k * tr, a.tw_scale, a.tw_mask);

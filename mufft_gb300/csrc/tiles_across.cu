@@ -21,6 +21,7 @@ void register_tiles_across(std::vector<TileKernel> &out)
     TILE(64, 16, 64);
     TILE(128, 16, 32);
     TILE(256, 16, 16);
+    TILE(256, 16, 32);
     TILE(512, 16, 8);
     TILE(1024, 16, 8);
     TILE(1024, 16, 16);

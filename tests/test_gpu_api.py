@@ -164,7 +164,7 @@ def test_plan_introspection(gpu):
     gpu.free_plan_1d(plan)
 
 
-@pytest.mark.parametrize("levels,fused,table", [(2, 1, -1), (3, 0, 0), (3, 0, 1), (3, 1, 0), (3, 1, 1)])
+@pytest.mark.parametrize("levels,fused,table", [(2, 1, -1), (2, 0, 1), (3, 0, 0), (3, 0, 1), (3, 0, 2), (3, 1, 0), (3, 1, 1)])
 @pytest.mark.parametrize("N,B", [(1 << 17, 2), (1 << 20, 3), (1 << 22, 1)])
 def test_multipass_variants(gpu, torch, levels, fused, table, N, B):
     """Every multi-pass schedule (four-step, three-level, fused last passes
