@@ -349,7 +349,216 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
     }
     if world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(N, B, threads=os.cpu_count() or 1)
+    if world == 1 and not args.no_companions:
+        del ins, outs
+        torch.cuda.empty_cache()
+        res["split_tc"] = companion_split(lib, torch)
+        res["ragged_conv"] = companion_ragged(lib, torch)
+        res["adjoint"] = companion_adjoint(lib, torch)
     return res
+
+
+# ------------------------------------------------------- companion measurements
+#
+# Measured once per run next to the headline (rank 0, one GPU), each on its
+# own workload: the split-precision tensor-core form against plain FP32, the
+# ragged batched convolution against per-request launches, and one
+# filter-fitting gradient step through the convolution adjoints.
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _time_ms(torch, fn, reps: int, warm: int = 2) -> float:
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = _events(torch)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def companion_split(lib, torch) -> dict:
+    """65536 x c2c N=4096: plain FP32 vs BF16x3 / BF16x2 split tensor-core
+    forms, time and error against FP64 on both input sets."""
+    from mufft_gb300 import capi as K
+    from mufft_gb300 import signals
+    N, B, sub = 4096, 65536, 128
+    sp = torch.cuda.current_stream().cuda_stream
+    x = torch.empty((B, N), dtype=torch.complex64, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x.real.uniform_(-1, 1, generator=g)
+    x.imag.uniform_(-1, 1, generator=g)
+    xa = signals.complex_uniform(3, sub * N).reshape(sub, N)
+    xb = signals.complex_logmag(3, sub * N).reshape(sub, N)
+    x[:sub] = torch.from_numpy(xa).cuda()
+    y = torch.empty_like(x)
+    refa = np.fft.fft(xa.astype(np.complex128), axis=1)
+    refb = np.fft.fft(xb.astype(np.complex128), axis=1)
+    dxb = torch.from_numpy(xb).cuda()
+    dyb = torch.empty_like(dxb)
+    out = {"workload": "c2c forward, batch 65536 x N=4096 complex64 (2 GiB in, 2 GiB out)",
+           "engines": "bf16x3 / bf16x2: tcgen05.mma with TMEM accumulators; bf16x3_mma_sync: warp-level mma.sync",
+           "sets": "A: re/im uniform [-1,1) (first 128 rows SplitMix64 seed 3, rest torch seed 3); "
+                   "B: magnitude log-uniform 1e-3..1e3, uniform phase (128 rows)"}
+    for name, flags, engine in (("fp32", 0, 0), ("bf16x3", K.FLAG_SPLIT_BF16X3, 0), ("bf16x2", K.FLAG_SPLIT_BF16X2, 0),
+                                ("bf16x3_mma_sync", K.FLAG_SPLIT_BF16X3, 1)):
+        lib.gb_set_split_engine(engine)
+        p = lib.gb_create_plan_1d_c2c_batched(N, -1, flags, B, 0, 0)
+        ps = lib.gb_create_plan_1d_c2c_batched(N, -1, flags, sub, 0, 0)
+        lib.gb_set_split_engine(0)
+        if not p or not ps:
+            raise RuntimeError(lib.gb_last_error_string().decode())
+        ms = _time_ms(torch, lambda: lib.gb_execute_plan_1d_async(p, y.data_ptr(), x.data_ptr(), sp), reps=10)
+        lib.gb_execute_plan_1d_async(ps, dyb.data_ptr(), dxb.data_ptr(), sp)
+        torch.cuda.synchronize()
+        ga, gb = y[:sub].cpu().numpy(), dyb.cpu().numpy()
+        out[name] = {"ms": ms, "GFLOP/s": 5.0 * N * 12 * B / (ms * 1e-3) / 1e9,
+                     "GB/s": 16.0 * N * B / (ms * 1e-3) / 1e9,
+                     "rel_l2_set_a": float(np.linalg.norm(ga - refa) / np.linalg.norm(refa)),
+                     "max_abs_set_a": float(np.abs(ga - refa).max()),
+                     "rel_l2_set_b": float(np.linalg.norm(gb - refb) / np.linalg.norm(refb)),
+                     "max_abs_set_b": float(np.abs(gb - refb).max())}
+        lib.free_plan_1d(p)
+        lib.free_plan_1d(ps)
+    out["bf16x3_time_vs_fp32"] = out["bf16x3"]["ms"] / out["fp32"]["ms"]
+    out["bf16x3_error_vs_fp32"] = out["bf16x3"]["rel_l2_set_a"] / out["fp32"]["rel_l2_set_a"]
+    del x, y
+    torch.cuda.empty_cache()
+    return out
+
+
+def _c4_requests(seed: int = 4, count: int = 512):
+    """Block sizes log-uniform 2^8..2^16, half stereo, filters N/2 taps of
+    N(0,1) x exp(-t/(N/8)), inputs N/2 samples uniform [-1,1)."""
+    from mufft_gb300 import signals
+    rng = np.random.default_rng(seed)
+    e = rng.integers(8, 17, count)
+    stereo = np.zeros(count, bool)
+    stereo[rng.permutation(count)[: count // 2]] = True
+    reqs = []
+    for i in range(count):
+        N = 1 << int(e[i])
+        t = np.arange(N // 2)
+        h = (signals.normal(10000 + i, N // 2) * np.exp(-t / (N / 8))).astype(np.float32)
+        x = (signals.complex_uniform(20000 + i, N // 2) if stereo[i] else signals.uniform(20000 + i, N // 2))
+        reqs.append((N, bool(stereo[i]), x, h))
+    return reqs
+
+
+def companion_ragged(lib, torch) -> dict:
+    from mufft_gb300 import capi as K
+    PADS = K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST | K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND
+    sp = torch.cuda.current_stream().cuda_stream
+    reqs = _c4_requests()
+    creq = (K.ConvRequest * len(reqs))()
+    plans, keep, seq, algo = {}, [], [], 0.0
+    for i, (N, stereo, x, h) in enumerate(reqs):
+        m = PADS | (1 if stereo else 0)
+        if (N, m) not in plans:
+            plans[(N, m)] = lib.create_plan_conv(N, 0, m)
+        p = plans[(N, m)]
+        nblk = lib.conv_get_transformed_block_size(p) // 8
+        hp = np.zeros(N, np.float32)
+        hp[: N // 2] = h
+        dh_time = torch.from_numpy(hp).cuda()
+        dH = torch.empty(nblk, dtype=torch.complex64, device="cuda")
+        assert lib.gb_execute_conv_input_async(p, K.CONV_BLOCK_SECOND, dH.data_ptr(), dh_time.data_ptr(), sp) == 0
+        din = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+        dspec = torch.empty(nblk, dtype=torch.complex64, device="cuda")
+        dout = torch.empty(N, dtype=torch.complex64 if stereo else torch.float32, device="cuda")
+        dseq = torch.empty_like(dout)
+        keep += [dh_time, dH, din, dspec, dout, dseq]
+        creq[i] = K.ConvRequest(N, m, din.data_ptr(), dH.data_ptr(), dout.data_ptr())
+        seq.append((p, din, dH, dspec, dseq))
+        algo += (14 if stereo else 8) * N
+    batch = lib.gb_create_conv_batch(creq, len(reqs), 0)
+    if not batch:
+        raise RuntimeError(lib.gb_last_error_string().decode())
+
+    def run_seq():
+        for p, din, dH, dspec, dseq in seq:
+            lib.gb_execute_conv_input_async(p, K.CONV_BLOCK_FIRST, dspec.data_ptr(), din.data_ptr(), sp)
+            lib.gb_execute_conv_output_async(p, dseq.data_ptr(), dspec.data_ptr(), dH.data_ptr(), sp)
+
+    ms_batch = _time_ms(torch, lambda: lib.gb_execute_conv_batch(batch, sp), reps=20)
+    ms_seq = _time_ms(torch, run_seq, reps=5)
+    # accuracy: every request against an FP64 linear convolution (zero padding
+    # makes the circular convolution of length N a linear one)
+    worst = 0.0
+    for i, (N, stereo, x, h) in enumerate(reqs):
+        got = keep[6 * i + 4].cpu().numpy()
+        ref = np.fft.ifft(np.fft.fft(np.asarray(x, np.complex128), N) * np.fft.fft(np.asarray(h, np.float64), N))
+        ref = ref if stereo else ref.real
+        worst = max(worst, float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    lib.gb_free_conv_batch(batch)
+    for p in plans.values():
+        lib.free_plan_conv(p)
+    return {"workload": "512 conv requests, N = 2^e with e ~ U{8..16}, 256 STEREO_MONO, N/2-sample inputs, "
+                        "N/2-tap filters (both zero-pad flags), seed 4",
+            "batch_ms": ms_batch, "sequential_ms": ms_seq, "speedup_vs_sequential": ms_seq / ms_batch,
+            "sequential": "per request mufft_gb_execute_conv_input_async(FIRST) + _conv_output_async on one stream",
+            "algorithmic_GB/s": algo / (ms_batch * 1e-3) / 1e9,
+            "worst_rel_l2_vs_fp64": worst}
+
+
+def companion_adjoint(lib, torch) -> dict:
+    """One filter-fitting gradient step: 64 stereo signals of 2^20 frames,
+    2^16 taps, N = 2^21 (zero-padded blocks make the convolution linear)."""
+    from mufft_gb300 import capi as K
+    B, L, T = 64, 1 << 20, 1 << 16
+    N = 2 * L
+    m = K.CONV_METHOD_FLAG_STEREO_MONO | K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST | \
+        K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND
+    sp = torch.cuda.current_stream().cuda_stream
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.zeros((B, N), dtype=torch.complex64, device="cuda")
+    x[:, :L].real.uniform_(-1, 1, generator=g)
+    x[:, :L].imag.uniform_(-1, 1, generator=g)
+    t = torch.arange(T, device="cuda", dtype=torch.float32)
+    h_hidden = torch.zeros(N, device="cuda")
+    h_hidden[:T] = torch.randn(T, device="cuda", generator=g) * torch.exp(-t / 8192)
+    h = torch.zeros(N, device="cuda")
+    h[:T] = torch.randn(T, device="cuda", generator=g) * torch.exp(-t / 8192)
+    plan = lib.create_plan_conv(N, 0, m)
+    nblk = lib.conv_get_transformed_block_size(plan) // 8
+    A = torch.empty((B, nblk), dtype=torch.complex64, device="cuda")
+    for b in range(B):  # first-block spectra, cached across steps
+        assert lib.gb_execute_conv_input_async(plan, K.CONV_BLOCK_FIRST, A[b].data_ptr(), x[b].data_ptr(), sp) == 0
+    H = torch.empty(nblk, dtype=torch.complex64, device="cuda")
+    ystar = torch.empty((B, N), dtype=torch.complex64, device="cuda")
+    lib.gb_execute_conv_input_async(plan, K.CONV_BLOCK_SECOND, H.data_ptr(), h_hidden.data_ptr(), sp)
+    for b in range(B):
+        lib.gb_execute_conv_output_async(plan, ystar[b].data_ptr(), A[b].data_ptr(), H.data_ptr(), sp)
+    y = torch.empty_like(ystar)
+    gx = torch.empty_like(ystar)
+    gh = torch.empty(N, device="cuda")
+    lr = 1e-7
+
+    def gd_step():
+        assert lib.gb_execute_conv_input_async(plan, K.CONV_BLOCK_SECOND, H.data_ptr(), h.data_ptr(), sp) == 0
+        for b in range(B):
+            lib.gb_execute_conv_output_async(plan, y[b].data_ptr(), A[b].data_ptr(), H.data_ptr(), sp)
+        y.sub_(ystar)  # residual r = conv(x, h) - y*
+        assert lib.gb_conv_adjoint_filter(plan, gh.data_ptr(), y.data_ptr(), N, A.data_ptr(), nblk, B, sp) == 0
+        for b in range(B):
+            lib.gb_conv_adjoint_input(plan, gx[b].data_ptr(), y[b].data_ptr(), H.data_ptr(), sp)
+        h[:T].sub_(lr * gh[:T])
+
+    ms = _time_ms(torch, gd_step, reps=5)
+    lib.free_plan_conv(plan)
+    fft_flops = 5.0 * N * math.log2(N) * (2 * B + 2 * B + 2)  # conv_output, adjoint input, gradient spectra, filter
+    del x, A, ystar, y, gx
+    torch.cuda.empty_cache()
+    return {"workload": "64 stereo signals x 2^20 frames, 2^16-tap filter, N = 2^21, loss 0.5||conv(x,h) - y*||^2",
+            "step_ms": ms,
+            "step": "filter spectrum + 64 conv_output + residual + filter adjoint (64 signals) + 64 input adjoints "
+                    "+ update; first-block spectra cached",
+            "fft_GFLOP/s": fft_flops / (ms * 1e-3) / 1e9}
 
 
 def run_reference(args, world, rank, pg) -> dict | None:
@@ -384,6 +593,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c_2^24")
     ap.add_argument("--batch", type=int, default=0, help="override the workload's batch (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-companions", action="store_true",
+                    help="skip the split-precision, ragged-convolution and adjoint measurements")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local, pg = dist_setup()

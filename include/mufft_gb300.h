@@ -202,6 +202,10 @@ int mufft_gb_set_multipass_levels(unsigned levels);
  * automatic choice (2 where the column tile has room, else 0).  Affects plans
  * created afterwards. */
 int mufft_gb_set_twiddle_table(int mode);
+/* Split-precision plans (MUFFT_GB_FLAG_SPLIT_*) created afterwards run their
+ * products on tcgen05.mma with TMEM accumulators (0, default) or on
+ * warp-level mma.sync (1). */
+int mufft_gb_set_split_engine(int engine);
 /* Three-level transforms of N1 x 65536 points run their last two passes as one
  * persistent launch whose intermediate stays in L2 (enable = 1) or as two
  * launches (0, default).  Affects plans created afterwards. */

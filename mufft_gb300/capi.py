@@ -89,6 +89,7 @@ GB_H = [
     ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
     ("conv_adjoint_input", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
+    ("set_split_engine", _i, [_i]),
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),
     ("free_conv_batch", None, [_vp]),

@@ -275,9 +275,9 @@ struct Pass {
     BcArgs bc{};
     size_t bc_counter_bytes = 0;
     unsigned bc_grid = 0;
-    // split-precision tensor-core transform (split_tc.cu)
+    // split-precision tensor-core transform (split_tc.cu, split_umma.cu)
     SplitArgs sp{};
-    int sp_stages = 0, sp_limbs = 0;
+    int sp_stages = 0, sp_limbs = 0, sp_engine = 0;
     unsigned sp_grid = 0;
 };
 
@@ -339,8 +339,12 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             a.in = (const float2 *)pick(p.in_role, b);
             a.out = (float2 *)pick(p.out_role, b);
             void *args[] = {&a};
-            cudaError_t e = cudaLaunchKernel(split_kernel(p.sp_stages, p.sp_limbs), dim3(p.sp_grid),
-                                             dim3(kSplitThreads), args, split_smem_bytes(), st);
+            cudaError_t e =
+                p.sp_engine == 0
+                    ? cudaLaunchKernel(split_umma_kernel(p.sp_stages, p.sp_limbs), dim3(p.sp_grid),
+                                       dim3(split_umma_threads()), args, split_umma_smem_bytes(), st)
+                    : cudaLaunchKernel(split_kernel(p.sp_stages, p.sp_limbs), dim3(p.sp_grid), dim3(kSplitThreads),
+                                       args, split_smem_bytes(), st);
             if (e != cudaSuccess)
                 return e;
         } else if (p.type == PASS_BC) {
@@ -389,8 +393,10 @@ std::string describe(const std::vector<Pass> &ps)
                      p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
                      p.a.conj);
         else if (p.type == PASS_SPLIT)
-            snprintf(buf, sizeof(buf), "%ssplit_tc N=%d bf16x%d grid=%u threads=%d smem=%zu conj=%d", i ? "; " : "",
-                     1 << (4 * p.sp_stages), p.sp_limbs, p.sp_grid, kSplitThreads, split_smem_bytes(), p.sp.conj);
+            snprintf(buf, sizeof(buf), "%ssplit_tc N=%d bf16x%d %s grid=%u threads=%d smem=%zu conj=%d", i ? "; " : "",
+                     1 << (4 * p.sp_stages), p.sp_limbs, p.sp_engine == 0 ? "tcgen05" : "mma.sync", p.sp_grid,
+                     p.sp_engine == 0 ? split_umma_threads() : kSplitThreads,
+                     p.sp_engine == 0 ? split_umma_smem_bytes() : split_smem_bytes(), p.sp.conj);
         else if (p.type == PASS_BC)
             snprintf(buf, sizeof(buf), "%sfused_bc 256x256 rows=%u blocks=%u ring=%u grid=%u", i ? "; " : "",
                      p.bc.n1, p.bc.nblk, p.bc.ring_slots, p.bc_grid);
@@ -427,12 +433,15 @@ struct PlanResources {
     int *err = nullptr;           // device error flag of bounded waits
     unsigned *afrag = nullptr;    // split precision: DFT-16 limbs in mma fragment order
     float2 *sptw = nullptr;       // split precision: stage twiddles
+    void *bfrag = nullptr;        // split precision (tcgen05): DFT-16 limbs as B operands
     void release()
     {
         cudaFree(afrag);
         cudaFree(sptw);
+        cudaFree(bfrag);
         afrag = nullptr;
         sptw = nullptr;
+        bfrag = nullptr;
         cudaFree(rtw);
         cudaFree(twlo);
         cudaFree(twlo2);
@@ -460,6 +469,8 @@ std::atomic<int> g_twiddle_table{-1};
 // default: the separate passes measured faster on GB300 -- they are bound by
 // instruction issue and latency, not by the HBM traffic the fusion saves).
 std::atomic<int> g_fused_bc{0};
+// Split-precision products on tcgen05.mma (0, default) or warp-level mma.sync (1).
+std::atomic<int> g_split_engine{0};
 
 bool use_twiddle_table(const TileKernel *k)
 {
@@ -1020,8 +1031,16 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
         p.sp.conj = direction == MUFFT_INVERSE ? 1 : 0;
         p.sp_stages = N == 256 ? 2 : 3;
         p.sp_limbs = split_limbs;
+        p.sp_engine = g_split_engine.load();
         const unsigned per_cta = kSplitPoints / N;
         p.sp_grid = (batch + per_cta - 1) / per_cta;
+        if (p.sp_engine == 0) {
+            // persistent: two CTAs per SM (152 SMs on GB300 when no device is queried)
+            int sms = 152;
+            if (!dry)
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, pl->device);
+            p.sp_grid = std::min(p.sp_grid, 2u * (unsigned)sms);
+        }
         if (!dry) {
             const std::vector<unsigned> af = split_afrag_table();
             if (!cuda_ok(cudaMalloc(&pl->res.afrag, af.size() * sizeof(unsigned)), "cudaMalloc(split table)") ||
@@ -1034,8 +1053,23 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
                 destroy_1d(pl);
                 return nullptr;
             }
+            const std::vector<unsigned short> bf = split_umma_bfrag_table();
+            if (!cuda_ok(cudaMalloc(&pl->res.bfrag, bf.size() * 2), "cudaMalloc(split table)") ||
+                !cuda_ok(cudaMemcpy(pl->res.bfrag, bf.data(), bf.size() * 2, cudaMemcpyHostToDevice),
+                         "cudaMemcpy(split table)") ||
+                !cuda_ok(cudaMalloc(&pl->res.err, sizeof(int)), "cudaMalloc(error flag)") ||
+                !cuda_ok(cudaMemset(pl->res.err, 0, sizeof(int)), "cudaMemset(error flag)") ||
+                !cuda_ok(cudaFuncSetAttribute(split_umma_kernel(p.sp_stages, split_limbs),
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)split_umma_smem_bytes()),
+                         "cudaFuncSetAttribute(split tcgen05)")) {
+                destroy_1d(pl);
+                return nullptr;
+            }
             p.sp.afrag = pl->res.afrag;
             p.sp.tw = pl->res.sptw;
+            p.sp.bfrag = pl->res.bfrag;
+            p.sp.err = pl->res.err;
         }
         pl->passes.push_back(p);
     } else if (!build_fft_passes(s, tw, pl->res, dry, pl->passes)) {
@@ -2001,6 +2035,16 @@ int mufft_gb_set_twiddle_table(int mode)
         return MUFFT_GB_ERR_INVALID;
     }
     g_twiddle_table.store(mode);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_split_engine(int engine)
+{
+    if (engine < 0 || engine > 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "engine must be 0 (tcgen05) or 1 (mma.sync)");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_split_engine.store(engine);
     return MUFFT_GB_OK;
 }
 

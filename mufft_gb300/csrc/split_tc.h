@@ -15,7 +15,9 @@ struct SplitArgs {
     unsigned ntrans;
     int conj;                     // 1: inverse (conjugate in and out)
     const unsigned *afrag;        // DFT-16 matrix limbs in mma A-fragment order
-    const float2 *tw;             // stage twiddles W_(16p)^(m*q): p = 16 at 0, p = 256 at 256
+    const float2 *tw;             // stage twiddle factors: W_256^(m*q) then W_4096^(m*r), m, q, r < 16
+    const void *bfrag;            // tcgen05 form: DFT-16 limbs as B operands (core-matrix order)
+    int *err;                     // tcgen05 form: set when a bounded wait times out
 };
 
 constexpr int kSplitThreads = 256;
@@ -28,5 +30,12 @@ size_t split_smem_bytes();
 // Im F, -Im F} x 32 lanes x 4 registers) and the stage twiddles.
 std::vector<unsigned> split_afrag_table();
 std::vector<float2> split_twiddle_table();
+
+// The same transforms with the products on tcgen05.mma (split_umma.cu):
+// persistent CTAs, grid = 2 x SMs at most.
+const void *split_umma_kernel(int stages, int limbs);
+size_t split_umma_smem_bytes();
+int split_umma_threads();
+std::vector<unsigned short> split_umma_bfrag_table();
 
 }  // namespace mgb

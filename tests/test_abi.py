@@ -83,11 +83,21 @@ def test_extension_flags_match_header():
 
 def test_split_precision_schedule_and_rejections(lib):
     buf = C.create_string_buffer(4096)
-    for N, limbs, flag in ((4096, 3, K.FLAG_SPLIT_BF16X3), (256, 2, K.FLAG_SPLIT_BF16X2)):
-        assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, buf, 4096) == 0
-        d = buf.value.decode()
-        assert d.startswith(f"split_tc N={N} bf16x{limbs}"), d
-        assert f"grid={65536 * N // 4096}" in d, d
+    try:
+        for N, limbs, flag in ((4096, 3, K.FLAG_SPLIT_BF16X3), (256, 2, K.FLAG_SPLIT_BF16X2)):
+            assert lib.gb_set_split_engine(1) == 0  # mma.sync: one CTA per 4096 points
+            assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, buf, 4096) == 0
+            d = buf.value.decode()
+            assert d.startswith(f"split_tc N={N} bf16x{limbs} mma.sync"), d
+            assert f"grid={65536 * N // 4096}" in d, d
+            assert lib.gb_set_split_engine(0) == 0  # tcgen05: persistent, two CTAs per SM
+            assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, buf, 4096) == 0
+            d = buf.value.decode()
+            assert d.startswith(f"split_tc N={N} bf16x{limbs} tcgen05 grid=304"), d
+    finally:
+        lib.gb_set_split_engine(0)
+    assert lib.gb_set_split_engine(2) == -1
+    lib.gb_clear_error()
     for N, kind, flags in ((1024, 0, K.FLAG_SPLIT_BF16X3), (4096, 1, K.FLAG_SPLIT_BF16X3),
                            (4096, 0, K.FLAG_SPLIT_BF16X2 | K.FLAG_ZERO_PAD_UPPER_HALF)):
         assert lib.gb_describe_schedule_1d(N, kind, K.FORWARD, flags, 1, buf, 4096) == -2, (N, kind, flags)

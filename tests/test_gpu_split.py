@@ -20,6 +20,13 @@ def gpu():
     return mufft_gb300.load()
 
 
+@pytest.fixture(params=[0, 1], ids=["tcgen05", "mma.sync"])
+def engine(request, gpu):
+    assert gpu.gb_set_split_engine(request.param) == 0
+    yield request.param
+    gpu.gb_set_split_engine(0)
+
+
 @pytest.fixture(scope="module")
 def torch():
     import torch as t
@@ -53,10 +60,10 @@ def inputs(kind, seed, B, N):
     return signals.complex_logmag(seed, B * N).reshape(B, N)  # magnitudes 1e-3..1e3
 
 
-@pytest.mark.parametrize("N,B", [(4096, 1), (4096, 37), (256, 1), (256, 100), (256, 4096)])
+@pytest.mark.parametrize("N,B", [(4096, 1), (4096, 37), (4096, 1000), (256, 1), (256, 100), (256, 4096)])
 @pytest.mark.parametrize("direction", [K.FORWARD, K.INVERSE])
 @pytest.mark.parametrize("kind", ["uniform", "logmag"])
-def test_split_bf16x3_matches_fp32_error(gpu, torch, N, B, direction, kind):
+def test_split_bf16x3_matches_fp32_error(gpu, torch, engine, N, B, direction, kind):
     x = inputs(kind, 40000 + N + B, B, N)
     ref = ref_f64(x, direction)
     split = run(gpu, torch, x, direction, K.FLAG_SPLIT_BF16X3)
@@ -70,7 +77,7 @@ def test_split_bf16x3_matches_fp32_error(gpu, torch, N, B, direction, kind):
 
 @pytest.mark.parametrize("N,B", [(4096, 9), (256, 64)])
 @pytest.mark.parametrize("kind", ["uniform", "logmag"])
-def test_split_bf16x2_error(gpu, torch, N, B, kind):
+def test_split_bf16x2_error(gpu, torch, engine, N, B, kind):
     x = inputs(kind, 41000 + N + B, B, N)
     for direction in (K.FORWARD, K.INVERSE):
         got = run(gpu, torch, x, direction, K.FLAG_SPLIT_BF16X2)
@@ -78,7 +85,7 @@ def test_split_bf16x2_error(gpu, torch, N, B, kind):
         assert 1e-7 < e < 5e-5, e  # two limbs: ~16 significant bits
 
 
-def test_split_strided_batch(gpu, torch):
+def test_split_strided_batch(gpu, torch, engine):
     """Padded batch distances go through the split path too."""
     N, B, dist = 4096, 5, 4096 + 64
     x = np.zeros((B, dist), np.complex64)
