@@ -38,6 +38,11 @@ extern "C" {
  *   BF16X2: two limbs, three products -- about 1e-5 relative error. */
 #define MUFFT_GB_FLAG_SPLIT_BF16X3 (1u << 24)
 #define MUFFT_GB_FLAG_SPLIT_BF16X2 (1u << 25)
+/* Plan creation first times the candidate schedules of this shape on the
+ * device (mufft_gb_autotune_1d) unless a choice for the shape is remembered;
+ * the fastest is used and remembered.  The reference chose its passes from a
+ * static table (fft.c:217-435); this flag makes the GPU choice measured. */
+#define MUFFT_GB_FLAG_AUTOTUNE (1u << 26)
 
 /* Last error of the calling thread (0 if none) and its text. */
 int mufft_gb_last_error(void);
@@ -202,6 +207,23 @@ int mufft_gb_set_multipass_levels(unsigned levels);
  * automatic choice (2 where the column tile has room, else 0).  Affects plans
  * created afterwards. */
 int mufft_gb_set_twiddle_table(int mode);
+/* --------------------------------------------------------- autotuning */
+
+/* Times the candidate GPU schedules of a 1D plan shape (kind 0 c2c, 1 r2c,
+ * 2 c2r; N, direction, flags and batch as for plan creation) on the current
+ * device -- pass count, inter-pass twiddle scheme, fused last passes, then
+ * every tile variant of the winning schedule's passes -- and remembers the
+ * fastest for plans of that shape created afterwards (by any entry point,
+ * including the reference's).  Allocates two N x batch complex buffers
+ * while it runs.  `report` (optional) receives one line per candidate. */
+int mufft_gb_autotune_1d(int kind, unsigned N, int direction, unsigned flags, unsigned batch, char *report,
+                         size_t report_size);
+/* The remembered choices as a text file, tied to the GPU model and SM count
+ * (loading a file made on another GPU fails with MUFFT_GB_ERR_INVALID). */
+int mufft_gb_autotune_save(const char *path);
+int mufft_gb_autotune_load(const char *path);
+void mufft_gb_autotune_clear(void);
+
 /* Split-precision plans (MUFFT_GB_FLAG_SPLIT_*) created afterwards run their
  * products on tcgen05.mma with TMEM accumulators (0, default) or on
  * warp-level mma.sync (1). */

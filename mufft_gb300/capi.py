@@ -27,6 +27,7 @@ FLAG_ZERO_PAD_UPPER_HALF = 1 << 17
 # mufft_gb300.h extension flags
 FLAG_SPLIT_BF16X3 = 1 << 24
 FLAG_SPLIT_BF16X2 = 1 << 25
+FLAG_AUTOTUNE = 1 << 26
 CONV_METHOD_FLAG_MONO_MONO = 0
 CONV_METHOD_FLAG_STEREO_MONO = 1
 CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST = 1 << 2
@@ -90,6 +91,10 @@ GB_H = [
     ("conv_adjoint_input", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
     ("set_split_engine", _i, [_i]),
+    ("autotune_1d", _i, [_i, _u, _i, _u, _u, _vp, _sz]),
+    ("autotune_save", _i, [C.c_char_p]),
+    ("autotune_load", _i, [C.c_char_p]),
+    ("autotune_clear", None, []),
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),
     ("free_conv_batch", None, [_vp]),

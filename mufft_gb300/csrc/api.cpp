@@ -22,7 +22,9 @@
 #include <cstring>
 #include <algorithm>
 #include <atomic>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -112,8 +114,25 @@ static std::vector<TileKernel> &tile_table()
 static std::mutex g_choice_mu;
 static std::vector<TileKernel> g_choice;  // preferred (L, lmap, smap) -> C
 
+// Schedule choices of one plan (the autotuner's unit): -2 leaves a knob at its
+// process-wide setting; `tiles` are preferred (L, lmap, smap) -> (C, R, Q).
+struct PlanOptions {
+    int levels = -2, twiddle = -2, fused = -2;
+    std::vector<TileKernel> tiles;
+};
+// Set while a plan is built with explicit choices (candidate or remembered).
+thread_local const PlanOptions *t_opts = nullptr;
+
 const TileKernel *find_tile(int L, int lmap, int smap, int C, int R, int Q)
 {
+    if (C == 0 && R == 0 && Q == 0 && t_opts) {
+        for (const TileKernel &k : t_opts->tiles)
+            if (k.L == L && k.lmap == lmap && k.smap == smap) {
+                C = k.C;
+                R = k.R;
+                Q = k.Q;
+            }
+    }
     if (C == 0 && R == 0 && Q == 0) {
         std::lock_guard<std::mutex> lock(g_choice_mu);
         for (const TileKernel &k : g_choice)
@@ -472,9 +491,13 @@ std::atomic<int> g_fused_bc{0};
 // Split-precision products on tcgen05.mma (0, default) or warp-level mma.sync (1).
 std::atomic<int> g_split_engine{0};
 
+int opt_twiddle() { return (t_opts && t_opts->twiddle != -2) ? t_opts->twiddle : g_twiddle_table.load(); }
+int opt_levels() { return (t_opts && t_opts->levels != -2) ? t_opts->levels : g_levels.load(); }
+int opt_fused() { return (t_opts && t_opts->fused != -2) ? t_opts->fused : g_fused_bc.load(); }
+
 bool use_twiddle_table(const TileKernel *k)
 {
-    const int t = g_twiddle_table.load();
+    const int t = opt_twiddle();
     return k->has_thi && t == 1;
 }
 
@@ -483,7 +506,7 @@ bool use_twiddle_table(const TileKernel *k)
 // thread times R per-column powers computed once per tile.
 bool use_colpow(const TileKernel *k)
 {
-    const int t = g_twiddle_table.load();
+    const int t = opt_twiddle();
     return k->has_thi && (t == 2 || t < 0);
 }
 
@@ -558,10 +581,10 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     }
 
     const unsigned lg = ilog2u(M);
-    int levels = g_levels.load();
+    int levels = opt_levels();
     if (levels == 0)
         levels = lg >= 22 ? 3 : 2;  // measured crossover on GB300
-    if (levels == 3 && lg >= 20 && g_fused_bc.load()) {
+    if (levels == 3 && lg >= 20 && opt_fused()) {
         // M = N1 x 65536: pass A column tiles of length N1, then the fused
         // persistent B/C launch with an L2-resident intermediate.
         const unsigned N1 = M >> 16;
@@ -905,6 +928,36 @@ void destroy_1d(mufft_plan_1d *pl)
     delete pl;
 }
 
+// ------------------------------------------------------------ autotune cache
+//
+// Remembered schedule choices per plan shape, filled by the autotuner
+// (mufft_gb_autotune_1d, or plan creation with MUFFT_GB_FLAG_AUTOTUNE) or
+// loaded from a file, and applied when a plan of that shape is created.
+struct TuneKey {
+    int kind;
+    unsigned N, batch, flags;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(kind, N, batch, flags) < std::tie(o.kind, o.N, o.batch, o.flags);
+    }
+};
+constexpr unsigned kTuneFlagMask = MUFFT_FLAG_FULL_R2C | MUFFT_FLAG_ZERO_PAD_UPPER_HALF;
+std::mutex g_tune_mu;
+std::map<TuneKey, PlanOptions> g_tune;
+
+bool tune_lookup(int kind, unsigned N, unsigned batch, unsigned flags, PlanOptions *o)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(TuneKey{kind, N, batch, flags & kTuneFlagMask});
+    if (it == g_tune.end())
+        return false;
+    *o = it->second;
+    return true;
+}
+
+bool autotune_run(int kind, unsigned N, int direction, unsigned flags, unsigned batch, PlanOptions *best,
+                  std::string *report);
+
 // prologue_override: PRO_MUL / PRO_MUL_C2R for convolution output plans.
 mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, unsigned batch,
                          size_t idist, size_t odist, int prologue_override, bool dry,
@@ -928,6 +981,8 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
         set_error(MUFFT_GB_ERR_INVALID, "batch must be >= 1");
         return nullptr;
     }
+    const bool autotune = (flags & MUFFT_GB_FLAG_AUTOTUNE) != 0;
+    flags &= ~MUFFT_GB_FLAG_AUTOTUNE;
     const bool zp = (flags & MUFFT_FLAG_ZERO_PAD_UPPER_HALF) != 0;
     const bool full = (flags & MUFFT_FLAG_FULL_R2C) != 0;
     const int split_limbs =
@@ -1072,9 +1127,26 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
             p.sp.err = pl->res.err;
         }
         pl->passes.push_back(p);
-    } else if (!build_fft_passes(s, tw, pl->res, dry, pl->passes)) {
-        destroy_1d(pl);
-        return nullptr;
+    } else {
+        // remembered (or, with MUFFT_GB_FLAG_AUTOTUNE, freshly tuned) schedule
+        // choices apply unless the plan is being built with explicit ones
+        PlanOptions tuned;
+        const PlanOptions *prev = t_opts;
+        if (!t_opts) {
+            bool have = tune_lookup(kind, N, batch, flags, &tuned);
+            if (!have && autotune && !dry) {
+                have = autotune_run(kind, N, direction, flags, batch, &tuned, nullptr);
+                t_err = 0;
+            }
+            if (have)
+                t_opts = &tuned;
+        }
+        const bool built = build_fft_passes(s, tw, pl->res, dry, pl->passes);
+        t_opts = prev;
+        if (!built) {
+            destroy_1d(pl);
+            return nullptr;
+        }
     }
     if (desc)
         *desc = describe(pl->passes);
@@ -1131,12 +1203,178 @@ int exec_1d(mufft_plan_1d *pl, void *out, const void *in, const void *in2, cudaS
     if (sync && pl->res.err) {
         int e = 0;
         if (cuda_ok(cudaMemcpy(&e, pl->res.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag") && e) {
-            set_error(MUFFT_GB_ERR_UNSUPPORTED, "a bounded wait in the fused passes timed out");
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "a bounded wait in a persistent kernel timed out");
             cudaMemset(pl->res.err, 0, sizeof(int));
             return t_err;
         }
     }
     return MUFFT_GB_OK;
+}
+
+std::string describe_options(const PlanOptions &o)
+{
+    std::string d;
+    char b[160];
+    snprintf(b, sizeof(b), "levels=%d twiddle=%d fused=%d", o.levels, o.twiddle, o.fused);
+    d = b;
+    for (const TileKernel &k : o.tiles) {
+        snprintf(b, sizeof(b), " tile(L=%d %s/%s C=%d R=%d Q=%d)", k.L, k.lmap ? "across" : "along",
+                 k.smap ? "across" : "along", k.C, k.R, k.Q);
+        d += b;
+    }
+    return d;
+}
+
+// Times the candidate schedules of one plan shape on the current device and
+// remembers the fastest.  Coordinate descent: the pass structure (levels,
+// twiddle scheme, fused last passes) with default tiles first, then each
+// tile role of the winner over its compiled variants.  Candidates run on
+// zero-filled scratch buffers; each time is the best of three groups of
+// back-to-back executes, measured with CUDA events.
+bool autotune_run(int kind, unsigned N, int direction, unsigned flags, unsigned batch, PlanOptions *best,
+                  std::string *report)
+{
+    const size_t bytes = (size_t)N * batch * sizeof(float2) + 256;
+    void *din = nullptr, *dout = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&] {
+        if (e0)
+            cudaEventDestroy(e0);
+        if (e1)
+            cudaEventDestroy(e1);
+        if (st)
+            cudaStreamDestroy(st);
+        cudaFree(din);
+        cudaFree(dout);
+    };
+    if (!cuda_ok(cudaMalloc(&din, bytes), "cudaMalloc(autotune)") ||
+        !cuda_ok(cudaMalloc(&dout, bytes), "cudaMalloc(autotune)") ||
+        !cuda_ok(cudaMemset(din, 0, bytes), "cudaMemset(autotune)") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&e1), "cudaEventCreate")) {
+        cleanup();
+        return false;
+    }
+    const size_t points = (size_t)N * batch;
+    const int reps = (int)std::max<size_t>(3, std::min<size_t>(20, ((size_t)1 << 26) / std::max<size_t>(points, 1)));
+    auto measure = [&](const PlanOptions &o, std::vector<TileKernel> *roles) -> double {
+        const PlanOptions *prev = t_opts;
+        t_opts = &o;
+        mufft_plan_1d *pl = create_1d(kind, N, direction, flags, batch, 0, 0, -1, false, nullptr);
+        t_opts = prev;
+        if (!pl) {
+            t_err = 0;
+            return INFINITY;
+        }
+        if (roles) {
+            roles->clear();
+            for (const Pass &p : pl->passes) {
+                if (p.type != PASS_TILE)
+                    continue;
+                bool seen = false;
+                for (const TileKernel &r : *roles)
+                    seen |= r.L == p.k->L && r.lmap == p.k->lmap && r.smap == p.k->smap;
+                if (!seen)
+                    roles->push_back(*p.k);
+            }
+        }
+        double ms = INFINITY;
+        bool ok = true;
+        for (int w = 0; w < 2 && ok; w++)
+            ok = exec_1d(pl, dout, din, nullptr, st, false) == MUFFT_GB_OK;
+        for (int g = 0; g < 3 && ok; g++) {
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && ok; r++)
+                ok = exec_1d(pl, dout, din, nullptr, st, false) == MUFFT_GB_OK;
+            cudaEventRecord(e1, st);
+            float t = 0.f;
+            ok = ok && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess;
+            if (ok)
+                ms = std::min(ms, (double)t / reps);
+        }
+        destroy_1d(pl);
+        if (!ok) {
+            cudaGetLastError();
+            t_err = 0;
+            return INFINITY;
+        }
+        if (report) {
+            char b[64];
+            snprintf(b, sizeof(b), "%.4f ms  ", ms);
+            *report += b + describe_options(o) + "\n";
+        }
+        return ms;
+    };
+    PlanOptions cur;
+    double cur_ms = measure(cur, nullptr);
+    const unsigned M = kind == K_C2C ? N : N / 2;
+    if (M <= (unsigned)kMaxSinglePass) {
+        for (const TileKernel &k : tile_table()) {
+            if (k.L != (int)M || k.lmap != ALONG || k.smap != ALONG)
+                continue;
+            PlanOptions o;
+            o.tiles = {k};
+            const double t = measure(o, nullptr);
+            if (t < cur_ms) {
+                cur = o;
+                cur_ms = t;
+            }
+        }
+    } else {
+        const unsigned lg = ilog2u(M);
+        for (int lv = 2; lv <= 3; lv++)
+            for (int tw = 0; tw <= 2; tw++)
+                for (int fu = 0; fu <= ((lv == 3 && lg >= 20) ? 1 : 0); fu++) {
+                    PlanOptions o;
+                    o.levels = lv;
+                    o.twiddle = tw;
+                    o.fused = fu;
+                    const double t = measure(o, nullptr);
+                    if (t < cur_ms) {
+                        cur = o;
+                        cur_ms = t;
+                    }
+                }
+        std::vector<TileKernel> roles;
+        measure(cur, &roles);
+        for (const TileKernel &role : roles) {
+            for (const TileKernel &k : tile_table()) {
+                if (k.L != role.L || k.lmap != role.lmap || k.smap != role.smap)
+                    continue;
+                PlanOptions o = cur;
+                bool replaced = false;
+                for (TileKernel &t : o.tiles)
+                    if (t.L == k.L && t.lmap == k.lmap && t.smap == k.smap) {
+                        t = k;
+                        replaced = true;
+                    }
+                if (!replaced)
+                    o.tiles.push_back(k);
+                const double t = measure(o, nullptr);
+                if (t < cur_ms) {
+                    cur = o;
+                    cur_ms = t;
+                }
+            }
+        }
+    }
+    cleanup();
+    if (!std::isfinite(cur_ms)) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "no schedule of this shape ran");
+        return false;
+    }
+    if (report) {
+        char b[64];
+        snprintf(b, sizeof(b), "best %.4f ms  ", cur_ms);
+        *report += b + describe_options(cur) + "\n";
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune[TuneKey{kind, N, batch, flags & kTuneFlagMask}] = cur;
+    }
+    *best = cur;
+    return true;
 }
 
 }  // namespace
@@ -2035,6 +2273,164 @@ int mufft_gb_set_twiddle_table(int mode)
         return MUFFT_GB_ERR_INVALID;
     }
     g_twiddle_table.store(mode);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_autotune_1d(int kind, unsigned N, int direction, unsigned flags, unsigned batch, char *report,
+                         size_t report_size)
+{
+    t_err = 0;
+    if (kind < 0 || kind > 2) {
+        set_error(MUFFT_GB_ERR_INVALID, "kind must be 0, 1 or 2");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (flags & (MUFFT_GB_FLAG_SPLIT_BF16X3 | MUFFT_GB_FLAG_SPLIT_BF16X2)) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "split-precision plans have a single schedule");
+        return MUFFT_GB_ERR_UNSUPPORTED;
+    }
+    flags &= ~MUFFT_GB_FLAG_AUTOTUNE;
+    // validate the shape the way plan creation does (no device work)
+    std::string dummy;
+    create_1d(kind, N, direction, flags, batch, 0, 0, -1, true, &dummy);
+    if (t_err)
+        return t_err;
+    int dev;
+    if (!device_prepare(&dev))
+        return t_err;
+    PlanOptions best;
+    std::string rep;
+    if (!autotune_run(kind, N, direction, flags, batch, &best, &rep))
+        return t_err ? t_err : MUFFT_GB_ERR_UNSUPPORTED;
+    t_err = 0;
+    if (report && report_size)
+        snprintf(report, report_size, "%s", rep.c_str());
+    return MUFFT_GB_OK;
+}
+
+void mufft_gb_autotune_clear(void)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune.clear();
+}
+
+namespace {
+
+bool device_identity(int *sms, std::string *name)
+{
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        set_error(MUFFT_GB_ERR_NO_DEVICE, "no CUDA device visible");
+        return false;
+    }
+    *sms = prop.multiProcessorCount;
+    *name = prop.name;
+    for (char &c : *name)
+        if (c == ' ' || c == '\t' || c == '\n')
+            c = '_';
+    return true;
+}
+
+}  // namespace
+
+// File format (text): a header line, the device line, then one line per shape:
+//   entry <kind> <N> <batch> <flags> <levels> <twiddle> <fused> <ntiles> {<L> <lmap> <smap> <C> <R> <Q>}
+int mufft_gb_autotune_save(const char *path)
+{
+    t_err = 0;
+    int sms;
+    std::string name;
+    if (!path) {
+        set_error(MUFFT_GB_ERR_INVALID, "null path");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (!device_identity(&sms, &name))
+        return t_err;
+    FILE *f = fopen(path, "w");
+    if (!f) {
+        set_error(MUFFT_GB_ERR_INVALID, "cannot write %s", path);
+        return MUFFT_GB_ERR_INVALID;
+    }
+    fprintf(f, "mufft_gb300-autotune 1\ndevice %d %s\n", sms, name.c_str());
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        for (const auto &kv : g_tune) {
+            const PlanOptions &o = kv.second;
+            fprintf(f, "entry %d %u %u %u %d %d %d %zu", kv.first.kind, kv.first.N, kv.first.batch, kv.first.flags,
+                    o.levels, o.twiddle, o.fused, o.tiles.size());
+            for (const TileKernel &k : o.tiles)
+                fprintf(f, " %d %d %d %d %d %d", k.L, k.lmap, k.smap, k.C, k.R, k.Q);
+            fprintf(f, "\n");
+        }
+    }
+    const bool ok = fclose(f) == 0;
+    if (!ok) {
+        set_error(MUFFT_GB_ERR_INVALID, "cannot write %s", path);
+        return MUFFT_GB_ERR_INVALID;
+    }
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_autotune_load(const char *path)
+{
+    t_err = 0;
+    int sms;
+    std::string name;
+    if (!path) {
+        set_error(MUFFT_GB_ERR_INVALID, "null path");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    FILE *f = fopen(path, "r");
+    if (!f) {
+        set_error(MUFFT_GB_ERR_INVALID, "cannot read %s", path);
+        return MUFFT_GB_ERR_INVALID;
+    }
+    char line[4096], fname[256];
+    int fsms = -1, version = 0;
+    bool ok = fgets(line, sizeof(line), f) && sscanf(line, "mufft_gb300-autotune %d", &version) == 1 && version == 1 &&
+              fgets(line, sizeof(line), f) && sscanf(line, "device %d %255s", &fsms, fname) == 2;
+    if (!ok) {
+        fclose(f);
+        set_error(MUFFT_GB_ERR_INVALID, "%s is not an autotune cache", path);
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (!device_identity(&sms, &name)) {
+        fclose(f);
+        return t_err;
+    }
+    if (fsms != sms || name != fname) {
+        fclose(f);
+        set_error(MUFFT_GB_ERR_INVALID, "autotune cache was made on another GPU (%s, %d SMs)", fname, fsms);
+        return MUFFT_GB_ERR_INVALID;
+    }
+    std::map<TuneKey, PlanOptions> loaded;
+    while (fgets(line, sizeof(line), f)) {
+        TuneKey k{};
+        PlanOptions o;
+        size_t nt = 0;
+        int used = 0;
+        if (sscanf(line, "entry %d %u %u %u %d %d %d %zu%n", &k.kind, &k.N, &k.batch, &k.flags, &o.levels,
+                   &o.twiddle, &o.fused, &nt, &used) != 8 || nt > 16)
+            continue;
+        const char *q = line + used;
+        bool good = true;
+        for (size_t i = 0; i < nt && good; i++) {
+            int L, lm, sm, C, R, Q, n = 0;
+            good = sscanf(q, "%d %d %d %d %d %d%n", &L, &lm, &sm, &C, &R, &Q, &n) == 6;
+            q += n;
+            const TileKernel *tk = good ? find_tile(L, lm, sm, C, R, Q) : nullptr;
+            good = tk && tk->C == C && tk->R == R && tk->Q == Q;
+            if (good)
+                o.tiles.push_back(*tk);
+        }
+        if (good)
+            loaded[k] = o;
+    }
+    fclose(f);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (const auto &kv : loaded)
+        g_tune[kv.first] = kv.second;
     return MUFFT_GB_OK;
 }
 

@@ -104,6 +104,27 @@ def test_split_precision_schedule_and_rejections(lib):
         lib.gb_clear_error()
 
 
+def test_autotune_argument_checks(lib, tmp_path):
+    buf = C.create_string_buffer(256)
+    assert lib.gb_autotune_1d(3, 1024, K.FORWARD, 0, 1, buf, 256) == -1
+    lib.gb_clear_error()
+    assert lib.gb_autotune_1d(0, 1000, K.FORWARD, 0, 1, buf, 256) == -1  # not a power of two
+    lib.gb_clear_error()
+    assert lib.gb_autotune_1d(0, 4096, K.FORWARD, K.FLAG_SPLIT_BF16X3, 1, buf, 256) == -2
+    lib.gb_clear_error()
+    assert lib.gb_autotune_load(str(tmp_path / "missing").encode()) == -1
+    junk = tmp_path / "junk.txt"
+    junk.write_text("not a cache\n")
+    assert lib.gb_autotune_load(str(junk).encode()) == -1
+    lib.gb_clear_error()
+    lib.gb_autotune_clear()
+    if not _has_gpu():
+        assert lib.gb_autotune_1d(0, 1 << 20, K.FORWARD, 0, 1, buf, 256) == -3
+        lib.gb_clear_error()
+    # the autotune flag alone changes nothing in a described schedule
+    assert _sched(lib, 1 << 20, 0, flags=K.FLAG_AUTOTUNE) == _sched(lib, 1 << 20, 0)
+
+
 def test_null_frees_are_noops(lib):
     lib.free_plan_1d(None)
     lib.free_plan_2d(None)
