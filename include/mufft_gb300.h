@@ -150,6 +150,36 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
 int mufft_gb_execute_conv_batch(mufft_gb_conv_batch *batch, void *stream);
 void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch);
 
+/* ---------------------------------------------- streaming convolution */
+
+/* A stream of `block`-sample blocks convolved with a filter of any length
+ * (the reference's block convolution, fft.c:794-809, extended to filters
+ * longer than a block): uniformly partitioned overlap-save.  The filter is
+ * cut into P = ceil(taps / block) partitions whose 2*block-point spectra are
+ * computed once here; each block costs one forward transform of the last two
+ * input blocks, a multiply-accumulate over the P partitions against the
+ * spectra of the last P windows, and one inverse transform -- one CUDA graph
+ * launch.  Output block k is samples k*block .. (k+1)*block - 1 of the linear
+ * convolution of the whole input stream with the filter.
+ *   method: MUFFT_CONV_METHOD_FLAG_MONO_MONO (real samples) or _STEREO_MONO
+ *     (complex samples: interleaved left/right); the filter is real.
+ *   filter: `taps` floats in host or device memory (copied here).
+ * No counterpart in the reference. */
+typedef struct mufft_gb_stream_conv mufft_gb_stream_conv;
+mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned method, const float *filter, unsigned taps,
+                                                  unsigned flags);
+/* Device buffer the next input block goes into (block floats or complex).
+ * Write it on the stream that runs mufft_gb_stream_conv_process, after the
+ * previous process call. */
+void *mufft_gb_stream_conv_input(mufft_gb_stream_conv *conv);
+/* Device buffer holding the last processed output block. */
+const void *mufft_gb_stream_conv_output(const mufft_gb_stream_conv *conv);
+/* Convolves the block in the input buffer (one graph launch on `stream`). */
+int mufft_gb_stream_conv_process(mufft_gb_stream_conv *conv, void *stream);
+/* Forgets the input history (as if the stream restarted from silence). */
+int mufft_gb_stream_conv_reset(mufft_gb_stream_conv *conv, void *stream);
+void mufft_gb_free_stream_conv(mufft_gb_stream_conv *conv);
+
 /* ------------------------------------------------- allocation-free execute */
 
 /* No counterpart in the reference.  A forward or inverse c2c transform of N

@@ -95,6 +95,12 @@ GB_H = [
     ("autotune_save", _i, [C.c_char_p]),
     ("autotune_load", _i, [C.c_char_p]),
     ("autotune_clear", None, []),
+    ("create_stream_conv", _vp, [_u, _u, _vp, _u, _u]),
+    ("stream_conv_input", _vp, [_vp]),
+    ("stream_conv_output", _vp, [_vp]),
+    ("stream_conv_process", _i, [_vp, _vp]),
+    ("stream_conv_reset", _i, [_vp, _vp]),
+    ("free_stream_conv", None, [_vp]),
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),
     ("free_conv_batch", None, [_vp]),

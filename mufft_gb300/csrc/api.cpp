@@ -1954,6 +1954,184 @@ void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch) { destroy_conv_batch(b
 
 }  // extern "C"
 
+// ======================================================= streaming convolution
+
+struct mufft_gb_stream_conv {
+    int device = -1;
+    unsigned block = 0, P = 0, nb = 0;
+    bool stereo = false;
+    mufft_plan_1d *fwd = nullptr, *inv = nullptr;
+    void *win = nullptr;      // 2 x block samples: previous block, then the caller's input
+    float2 *xcur = nullptr;   // spectrum of the current window (nb bins)
+    float2 *fdl = nullptr;    // P x nb: spectra of the last P windows
+    float2 *h = nullptr;      // P x nb: filter-partition spectra
+    float2 *y = nullptr;      // nb bins of the output spectrum
+    void *ybuf = nullptr;     // 2 x block samples of the inverse; the output is the second half
+    unsigned *counter = nullptr;  // [0] blocks processed, [1] CTA ticket
+    cudaStream_t capture = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void destroy_stream_conv(mufft_gb_stream_conv *c)
+{
+    if (!c)
+        return;
+    destroy_1d(c->fwd);
+    destroy_1d(c->inv);
+    if (c->device >= 0) {
+        DeviceGuard g(c->device);
+        if (c->exec)
+            cudaGraphExecDestroy(c->exec);
+        if (c->capture)
+            cudaStreamDestroy(c->capture);
+        cudaFree(c->win);
+        cudaFree(c->xcur);
+        cudaFree(c->fdl);
+        cudaFree(c->h);
+        cudaFree(c->y);
+        cudaFree(c->ybuf);
+        cudaFree(c->counter);
+    }
+    delete c;
+}
+
+}  // namespace
+
+extern "C" {
+
+mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned method, const float *filter, unsigned taps,
+                                                  unsigned flags)
+{
+    t_err = 0;
+    if (!is_pow2(block) || block < 2 || block > (1u << 23) || !filter || taps == 0) {
+        set_error(MUFFT_GB_ERR_INVALID, "block must be a power of two in 2..2^23 and the filter non-empty");
+        return nullptr;
+    }
+    const bool stereo = (method & 1u) == MUFFT_CONV_METHOD_FLAG_STEREO_MONO;
+    const unsigned L = 2 * block;
+    const unsigned P = (taps + block - 1) / block;
+    const unsigned nb = stereo ? L : block + 1;
+    const unsigned tflags = flags & ~(unsigned)(MUFFT_FLAG_ZERO_PAD_UPPER_HALF | MUFFT_FLAG_FULL_R2C);
+    mufft_gb_stream_conv *c = new mufft_gb_stream_conv();
+    c->block = block;
+    c->P = P;
+    c->nb = nb;
+    c->stereo = stereo;
+    c->fwd = create_1d(stereo ? K_C2C : K_R2C, L, MUFFT_FORWARD, tflags, 1, 0, 0, -1, false, nullptr);
+    c->inv = create_1d(stereo ? K_C2C : K_C2R, L, MUFFT_INVERSE, tflags, 1, 0, 0, -1, false, nullptr);
+    if (!c->fwd || !c->inv) {
+        destroy_stream_conv(c);
+        return nullptr;
+    }
+    c->device = c->fwd->device;
+    DeviceGuard g(c->device);
+    const size_t sample = stereo ? sizeof(float2) : sizeof(float);
+    // filter partitions: P zero-padded windows of L reals, transformed as one batch
+    mufft_plan_1d *hp = create_1d(K_R2C, L, MUFFT_FORWARD, tflags | (stereo ? MUFFT_FLAG_FULL_R2C : 0), P,
+                                  L, nb, -1, false, nullptr);
+    float *hpad = nullptr;
+    bool ok = hp && cuda_ok(cudaMalloc(&c->win, 2 * (size_t)block * sample), "cudaMalloc(window)") &&
+              cuda_ok(cudaMalloc(&c->xcur, (size_t)nb * sizeof(float2)), "cudaMalloc(spectrum)") &&
+              cuda_ok(cudaMalloc(&c->fdl, (size_t)P * nb * sizeof(float2)), "cudaMalloc(delay line)") &&
+              cuda_ok(cudaMalloc(&c->h, (size_t)P * nb * sizeof(float2)), "cudaMalloc(filter spectra)") &&
+              cuda_ok(cudaMalloc(&c->y, (size_t)nb * sizeof(float2)), "cudaMalloc(output spectrum)") &&
+              cuda_ok(cudaMalloc(&c->ybuf, 2 * (size_t)block * sample), "cudaMalloc(output)") &&
+              cuda_ok(cudaMalloc(&c->counter, 2 * sizeof(unsigned)), "cudaMalloc(counter)") &&
+              cuda_ok(cudaMalloc(&hpad, (size_t)P * L * sizeof(float)), "cudaMalloc(partitions)") &&
+              cuda_ok(cudaMemset(hpad, 0, (size_t)P * L * sizeof(float)), "cudaMemset") &&
+              cuda_ok(cudaMemset(c->win, 0, 2 * (size_t)block * sample), "cudaMemset") &&
+              cuda_ok(cudaMemset(c->fdl, 0, (size_t)P * nb * sizeof(float2)), "cudaMemset") &&
+              cuda_ok(cudaMemset(c->counter, 0, 2 * sizeof(unsigned)), "cudaMemset");
+    // partition p = filter[p*block .. (p+1)*block) at the start of window p
+    for (unsigned p = 0; ok && p < P; p++) {
+        const unsigned n = std::min(block, taps - p * block);
+        ok = cuda_ok(cudaMemcpy(hpad + (size_t)p * L, filter + (size_t)p * block, n * sizeof(float), cudaMemcpyDefault),
+                     "cudaMemcpy(filter)");
+    }
+    ok = ok && exec_1d(hp, c->h, hpad, nullptr, nullptr, false) == MUFFT_GB_OK &&
+         cuda_ok(cudaDeviceSynchronize(), "filter spectra");
+    destroy_1d(hp);
+    cudaFree(hpad);
+    if (!ok) {
+        destroy_stream_conv(c);
+        return nullptr;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    // one block: spectrum of [previous, input], multiply-accumulate, inverse,
+    // then the input becomes the previous block
+    cudaGraph_t gr = nullptr;
+    ok = cuda_ok(cudaStreamCreateWithFlags(&c->capture, cudaStreamNonBlocking), "cudaStreamCreate") &&
+         cuda_ok(cudaStreamBeginCapture(c->capture, cudaStreamCaptureModeThreadLocal), "capture");
+    if (ok) {
+        const bool body = exec_1d(c->fwd, c->xcur, c->win, nullptr, c->capture, false) == MUFFT_GB_OK &&
+                          cuda_ok(launch_upols_mac(c->y, c->xcur, c->fdl, c->h, nb, P, c->counter, c->counter + 1,
+                                                   1.0f / (float)L, sms, c->capture),
+                                  "multiply-accumulate") &&
+                          exec_1d(c->inv, c->ybuf, c->y, nullptr, c->capture, false) == MUFFT_GB_OK &&
+                          cuda_ok(cudaMemcpyAsync(c->win, (char *)c->win + (size_t)block * sample,
+                                                  (size_t)block * sample, cudaMemcpyDeviceToDevice, c->capture),
+                                  "window shift");
+        const cudaError_t ce = cudaStreamEndCapture(c->capture, &gr);
+        ok = body && cuda_ok(ce, "capture") && cuda_ok(cudaGraphInstantiate(&c->exec, gr, 0), "cudaGraphInstantiate");
+        if (gr)
+            cudaGraphDestroy(gr);
+    }
+    if (!ok) {
+        destroy_stream_conv(c);
+        return nullptr;
+    }
+    return c;
+}
+
+void *mufft_gb_stream_conv_input(mufft_gb_stream_conv *c)
+{
+    if (!c)
+        return nullptr;
+    return (char *)c->win + (size_t)c->block * (c->stereo ? sizeof(float2) : sizeof(float));
+}
+
+const void *mufft_gb_stream_conv_output(const mufft_gb_stream_conv *c)
+{
+    if (!c)
+        return nullptr;
+    return (const char *)c->ybuf + (size_t)c->block * (c->stereo ? sizeof(float2) : sizeof(float));
+}
+
+int mufft_gb_stream_conv_process(mufft_gb_stream_conv *c, void *stream)
+{
+    if (!c) {
+        set_error(MUFFT_GB_ERR_INVALID, "null convolver");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(c->device);
+    if (!cuda_ok(cudaGraphLaunch(c->exec, (cudaStream_t)stream), "cudaGraphLaunch"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_stream_conv_reset(mufft_gb_stream_conv *c, void *stream)
+{
+    if (!c) {
+        set_error(MUFFT_GB_ERR_INVALID, "null convolver");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(c->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    const size_t sample = c->stereo ? sizeof(float2) : sizeof(float);
+    if (!cuda_ok(cudaMemsetAsync(c->win, 0, 2 * (size_t)c->block * sample, st), "reset") ||
+        !cuda_ok(cudaMemsetAsync(c->fdl, 0, (size_t)c->P * c->nb * sizeof(float2), st), "reset") ||
+        !cuda_ok(cudaMemsetAsync(c->counter, 0, 2 * sizeof(unsigned), st), "reset"))
+        return t_err;
+    return MUFFT_GB_OK;
+}
+
+void mufft_gb_free_stream_conv(mufft_gb_stream_conv *c) { destroy_stream_conv(c); }
+
+}  // extern "C"
+
 // ================================================================== 2D
 
 enum Kind2D { K2_C2C = 0, K2_R2C = 1, K2_C2R = 2 };

@@ -85,6 +85,42 @@ __global__ void adjoint_filter_reduce(float2 *acc, const float2 *__restrict__ g,
     }
 }
 
+// Uniformly partitioned overlap-save, one block k: multiply-accumulate of
+// the current input spectrum and the previous P-1 ones (a ring of P slots,
+// block j in slot j % P) with the P filter-partition spectra, scaled; the
+// current spectrum then replaces block k-P in the ring.  `counter` holds k;
+// the last CTA to finish advances it (a ticket on `done`, no waiting).
+__global__ void upols_mac(float2 *__restrict__ y, const float2 *__restrict__ xcur, float2 *fdl,
+                          const float2 *__restrict__ h, unsigned nb, unsigned P, unsigned *counter,
+                          unsigned *done, float s)
+{
+    const unsigned k = *(volatile unsigned *)counter;
+    const unsigned cur = k % P;
+    for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const float2 x = xcur[b];
+        float2 acc = cmul(x, h[b]);
+        unsigned slot = cur;
+        for (unsigned p = 1; p < P; p++) {
+            slot = slot ? slot - 1 : P - 1;  // block k - p
+            const float2 xp = fdl[(size_t)slot * nb + b];
+            const float2 hp = h[(size_t)p * nb + b];
+            acc.x += xp.x * hp.x - xp.y * hp.y;
+            acc.y += xp.x * hp.y + xp.y * hp.x;
+        }
+        fdl[(size_t)cur * nb + b] = x;
+        y[b] = make_float2(acc.x * s, acc.y * s);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(done, 1u) == gridDim.x - 1) {
+            *done = 0;
+            *counter = k + 1;
+            __threadfence();
+        }
+    }
+}
+
 __global__ void fill_u32(unsigned *p, unsigned v, unsigned long long n)
 {
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
@@ -124,6 +160,16 @@ cudaError_t launch_adjoint_filter_reduce(float2 *acc, const float2 *g, long long
     if (blocks > 8192)
         blocks = 8192;
     adjoint_filter_reduce<<<blocks, 256, 0, st>>>(acc, g, gdist, a, adist, count, N, stereo, s, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_upols_mac(float2 *y, const float2 *xcur, float2 *fdl, const float2 *h, unsigned nb, unsigned P,
+                             unsigned *counter, unsigned *done, float s, int sms, cudaStream_t st)
+{
+    unsigned blocks = (nb + 255) / 256;
+    const unsigned cap = 4u * (unsigned)(sms > 0 ? sms : 152);
+    blocks = blocks > cap ? cap : (blocks ? blocks : 1);
+    upols_mac<<<blocks, 256, 0, st>>>(y, xcur, fdl, h, nb, P, counter, done, s);
     return cudaGetLastError();
 }
 

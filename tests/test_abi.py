@@ -125,6 +125,19 @@ def test_autotune_argument_checks(lib, tmp_path):
     assert _sched(lib, 1 << 20, 0, flags=K.FLAG_AUTOTUNE) == _sched(lib, 1 << 20, 0)
 
 
+def test_stream_conv_validates_on_host(lib):
+    import numpy as np
+    h = np.ones(10, np.float32)
+    for block, taps in ((1000, 10), (1, 10), (256, 0)):
+        assert not lib.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0)
+        assert lib.gb_last_error() == -1
+        lib.gb_clear_error()
+    assert not lib.gb_stream_conv_input(None) and not lib.gb_stream_conv_output(None)
+    assert lib.gb_stream_conv_process(None, None) == -1
+    lib.gb_clear_error()
+    lib.gb_free_stream_conv(None)
+
+
 def test_null_frees_are_noops(lib):
     lib.free_plan_1d(None)
     lib.free_plan_2d(None)

@@ -1,0 +1,91 @@
+"""GPU tests of the streaming partitioned convolution
+(mufft_gb_create_stream_conv): a stream of blocks convolved with filters
+shorter and much longer than a block, against the FP64 linear convolution of
+the whole stream."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+from mufft_gb300 import capi as K
+from mufft_gb300 import signals
+
+pytestmark = pytest.mark.gpu
+STEREO = K.CONV_METHOD_FLAG_STEREO_MONO
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import mufft_gb300
+    return mufft_gb300.load()
+
+
+def linear_conv_f64(x, h):
+    n = len(x) + len(h) - 1
+    L = 1 << (n - 1).bit_length()
+    return np.fft.ifft(np.fft.fft(x.astype(np.complex128), L) * np.fft.fft(h.astype(np.float64), L))[: len(x)]
+
+
+def stream(gpu, block, method, h, x, restart_at=None):
+    stereo = method & 1
+    conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, len(h), 0)
+    assert conv, gpu.gb_last_error_string()
+    sample = 8 if stereo else 4
+    out = np.zeros(len(x), np.complex64 if stereo else np.float32)
+    try:
+        inp, outp = gpu.gb_stream_conv_input(conv), gpu.gb_stream_conv_output(conv)
+        for k in range(len(x) // block):
+            if restart_at is not None and k == restart_at:
+                assert gpu.gb_stream_conv_reset(conv, None) == 0
+            blk = np.ascontiguousarray(x[k * block:(k + 1) * block])
+            assert gpu.gb_memcpy(inp, blk.ctypes.data, block * sample) == 0
+            assert gpu.gb_stream_conv_process(conv, None) == 0, gpu.gb_last_error_string()
+            assert gpu.gb_memcpy(out[k * block:].ctypes.data, outp, block * sample) == 0
+    finally:
+        gpu.gb_free_stream_conv(conv)
+    return out
+
+
+@pytest.mark.parametrize("block", [64, 1024])
+@pytest.mark.parametrize("taps_of", [lambda b: 1, lambda b: 100, lambda b: b, lambda b: 3 * b + 5, lambda b: 40 * b])
+@pytest.mark.parametrize("method", [0, STEREO])
+def test_stream_conv_matches_linear_convolution(gpu, block, taps_of, method):
+    taps = taps_of(block)
+    blocks = 12
+    h = (signals.normal(60000 + taps, taps) * np.exp(-np.arange(taps) / max(1.0, taps / 4))).astype(np.float32)
+    n = blocks * block
+    x = signals.complex_uniform(61000 + block, n) if method & 1 else signals.uniform(61000 + block, n)
+    got = stream(gpu, block, method, h, x)
+    ref = linear_conv_f64(x, h)
+    if not method & 1:
+        ref = ref.real
+    assert rel_l2(got, ref) < 1e-5, (block, taps, method)
+
+
+def test_stream_conv_long_filter(gpu):
+    """2^20 taps in 256 partitions of 4096."""
+    block, taps = 4096, 1 << 20
+    h = (signals.normal(62000, taps) * np.exp(-np.arange(taps) / (taps / 8))).astype(np.float32)
+    x = signals.uniform(62001, 8 * block)
+    got = stream(gpu, block, 0, h, x)
+    assert rel_l2(got, linear_conv_f64(x, h).real) < 1e-5
+
+
+def test_stream_conv_reset_restarts_history(gpu):
+    block, taps = 256, 1000
+    h = signals.normal(63000, taps).astype(np.float32)
+    x = signals.uniform(63001, 6 * block)
+    xx = np.concatenate([x, x])
+    got = stream(gpu, block, 0, h, xx, restart_at=6)
+    assert np.array_equal(got[: 6 * block].view(np.uint32), got[6 * block:].view(np.uint32))
+
+
+def test_stream_conv_rejects_bad_arguments(gpu):
+    h = np.ones(10, np.float32)
+    for block, taps in ((1000, 10), (1, 10), (256, 0)):
+        assert not gpu.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0)
+        assert gpu.gb_last_error() == -1
+        gpu.gb_clear_error()
