@@ -1967,7 +1967,10 @@ struct mufft_gb_stream_conv {
     float2 *h = nullptr;      // P x nb: filter-partition spectra
     float2 *y = nullptr;      // nb bins of the output spectrum
     void *ybuf = nullptr;     // 2 x block samples of the inverse; the output is the second half
-    unsigned *counter = nullptr;  // [0] blocks processed, [1] CTA ticket
+    float2 *part = nullptr;   // G x nb partial sums of the multiply-accumulate
+    unsigned G = 1;           // partition ranges per bin column
+    unsigned *counter = nullptr;  // [0] blocks processed, [1] CTA ticket, [2 + x] bin-column tickets
+    size_t counter_bytes = 0;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -1992,6 +1995,7 @@ void destroy_stream_conv(mufft_gb_stream_conv *c)
         cudaFree(c->h);
         cudaFree(c->y);
         cudaFree(c->ybuf);
+        cudaFree(c->part);
         cudaFree(c->counter);
     }
     delete c;
@@ -2031,6 +2035,10 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
     // filter partitions: P zero-padded windows of L reals, transformed as one batch
     mufft_plan_1d *hp = create_1d(K_R2C, L, MUFFT_FORWARD, tflags | (stereo ? MUFFT_FLAG_FULL_R2C : 0), P,
                                   L, nb, -1, false, nullptr);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->G = upols_chunks(nb, P, sms);
+    c->counter_bytes = (2 + (nb + 255) / 256) * sizeof(unsigned);
     float *hpad = nullptr;
     bool ok = hp && cuda_ok(cudaMalloc(&c->win, 2 * (size_t)block * sample), "cudaMalloc(window)") &&
               cuda_ok(cudaMalloc(&c->xcur, (size_t)nb * sizeof(float2)), "cudaMalloc(spectrum)") &&
@@ -2038,12 +2046,13 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
               cuda_ok(cudaMalloc(&c->h, (size_t)P * nb * sizeof(float2)), "cudaMalloc(filter spectra)") &&
               cuda_ok(cudaMalloc(&c->y, (size_t)nb * sizeof(float2)), "cudaMalloc(output spectrum)") &&
               cuda_ok(cudaMalloc(&c->ybuf, 2 * (size_t)block * sample), "cudaMalloc(output)") &&
-              cuda_ok(cudaMalloc(&c->counter, 2 * sizeof(unsigned)), "cudaMalloc(counter)") &&
+              cuda_ok(cudaMalloc(&c->part, (size_t)c->G * nb * sizeof(float2)), "cudaMalloc(partials)") &&
+              cuda_ok(cudaMalloc(&c->counter, c->counter_bytes), "cudaMalloc(counter)") &&
               cuda_ok(cudaMalloc(&hpad, (size_t)P * L * sizeof(float)), "cudaMalloc(partitions)") &&
               cuda_ok(cudaMemset(hpad, 0, (size_t)P * L * sizeof(float)), "cudaMemset") &&
               cuda_ok(cudaMemset(c->win, 0, 2 * (size_t)block * sample), "cudaMemset") &&
               cuda_ok(cudaMemset(c->fdl, 0, (size_t)P * nb * sizeof(float2)), "cudaMemset") &&
-              cuda_ok(cudaMemset(c->counter, 0, 2 * sizeof(unsigned)), "cudaMemset");
+              cuda_ok(cudaMemset(c->counter, 0, c->counter_bytes), "cudaMemset");
     // partition p = filter[p*block .. (p+1)*block) at the start of window p
     for (unsigned p = 0; ok && p < P; p++) {
         const unsigned n = std::min(block, taps - p * block);
@@ -2058,8 +2067,6 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
         destroy_stream_conv(c);
         return nullptr;
     }
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     // one block: spectrum of [previous, input], multiply-accumulate, inverse,
     // then the input becomes the previous block
     cudaGraph_t gr = nullptr;
@@ -2067,8 +2074,8 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
          cuda_ok(cudaStreamBeginCapture(c->capture, cudaStreamCaptureModeThreadLocal), "capture");
     if (ok) {
         const bool body = exec_1d(c->fwd, c->xcur, c->win, nullptr, c->capture, false) == MUFFT_GB_OK &&
-                          cuda_ok(launch_upols_mac(c->y, c->xcur, c->fdl, c->h, nb, P, c->counter, c->counter + 1,
-                                                   1.0f / (float)L, sms, c->capture),
+                          cuda_ok(launch_upols_mac(c->y, c->xcur, c->fdl, c->h, c->part, nb, P, c->G, c->counter,
+                                                   1.0f / (float)L, c->capture),
                                   "multiply-accumulate") &&
                           exec_1d(c->inv, c->ybuf, c->y, nullptr, c->capture, false) == MUFFT_GB_OK &&
                           cuda_ok(cudaMemcpyAsync(c->win, (char *)c->win + (size_t)block * sample,
@@ -2123,7 +2130,7 @@ int mufft_gb_stream_conv_reset(mufft_gb_stream_conv *c, void *stream)
     const size_t sample = c->stereo ? sizeof(float2) : sizeof(float);
     if (!cuda_ok(cudaMemsetAsync(c->win, 0, 2 * (size_t)c->block * sample, st), "reset") ||
         !cuda_ok(cudaMemsetAsync(c->fdl, 0, (size_t)c->P * c->nb * sizeof(float2), st), "reset") ||
-        !cuda_ok(cudaMemsetAsync(c->counter, 0, 2 * sizeof(unsigned), st), "reset"))
+        !cuda_ok(cudaMemsetAsync(c->counter, 0, c->counter_bytes, st), "reset"))
         return t_err;
     return MUFFT_GB_OK;
 }

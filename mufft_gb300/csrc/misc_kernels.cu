@@ -88,35 +88,60 @@ __global__ void adjoint_filter_reduce(float2 *acc, const float2 *__restrict__ g,
 // Uniformly partitioned overlap-save, one block k: multiply-accumulate of
 // the current input spectrum and the previous P-1 ones (a ring of P slots,
 // block j in slot j % P) with the P filter-partition spectra, scaled; the
-// current spectrum then replaces block k-P in the ring.  `counter` holds k;
-// the last CTA to finish advances it (a ticket on `done`, no waiting).
+// current spectrum then replaces block k-P in the ring.  CTAs tile
+// (256 bins) x (a range of partitions) so that long filters spread over the
+// whole GPU; each writes a partial sum, and the last CTA of a bin column
+// (ticket) adds the partials in partition order (deterministic).  The last
+// CTA overall advances the block counter.  Tickets never wait.
+//   tickets[0] = k, tickets[1] = CTAs done, tickets[2 + x] = column x done.
 __global__ void upols_mac(float2 *__restrict__ y, const float2 *__restrict__ xcur, float2 *fdl,
-                          const float2 *__restrict__ h, unsigned nb, unsigned P, unsigned *counter,
-                          unsigned *done, float s)
+                          const float2 *__restrict__ h, float2 *part, unsigned nb, unsigned P, unsigned *tickets,
+                          float s)
 {
-    const unsigned k = *(volatile unsigned *)counter;
+    __shared__ unsigned s_last;
+    const unsigned k = *(volatile unsigned *)&tickets[0];
     const unsigned cur = k % P;
-    for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    const unsigned G = gridDim.y, g = blockIdx.y;
+    const unsigned p0 = (unsigned)((unsigned long long)P * g / G), p1 = (unsigned)((unsigned long long)P * (g + 1) / G);
+    const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nb) {
         const float2 x = xcur[b];
-        float2 acc = cmul(x, h[b]);
-        unsigned slot = cur;
-        for (unsigned p = 1; p < P; p++) {
-            slot = slot ? slot - 1 : P - 1;  // block k - p
-            const float2 xp = fdl[(size_t)slot * nb + b];
+        float2 acc = make_float2(0.f, 0.f);
+        for (unsigned p = p0; p < p1; p++) {
+            const unsigned slot = (cur + P - p) % P;  // block k - p
+            const float2 xp = p == 0 ? x : fdl[(size_t)slot * nb + b];
             const float2 hp = h[(size_t)p * nb + b];
             acc.x += xp.x * hp.x - xp.y * hp.y;
             acc.y += xp.x * hp.y + xp.y * hp.x;
         }
-        fdl[(size_t)cur * nb + b] = x;
-        y[b] = make_float2(acc.x * s, acc.y * s);
+        part[(size_t)g * nb + b] = acc;
+        if (g == 0)
+            fdl[(size_t)cur * nb + b] = x;  // slot of block k - P: no CTA reads it for block k
     }
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0)
+        s_last = atomicAdd(&tickets[2 + blockIdx.x], 1u) == G - 1;
+    __syncthreads();
+    if (s_last) {
         __threadfence();
-        if (atomicAdd(done, 1u) == gridDim.x - 1) {
-            *done = 0;
-            *counter = k + 1;
+        if (b < nb) {
+            float2 acc = make_float2(0.f, 0.f);
+            for (unsigned q = 0; q < G; q++) {
+                const float2 v = __ldcg(&part[(size_t)q * nb + b]);
+                acc.x += v.x;
+                acc.y += v.y;
+            }
+            y[b] = make_float2(acc.x * s, acc.y * s);
+        }
+        if (threadIdx.x == 0) {
+            tickets[2 + blockIdx.x] = 0;
             __threadfence();
+            if (atomicAdd(&tickets[1], 1u) == gridDim.x - 1) {
+                tickets[1] = 0;
+                tickets[0] = k + 1;
+                __threadfence();
+            }
         }
     }
 }
@@ -163,14 +188,20 @@ cudaError_t launch_adjoint_filter_reduce(float2 *acc, const float2 *g, long long
     return cudaGetLastError();
 }
 
-cudaError_t launch_upols_mac(float2 *y, const float2 *xcur, float2 *fdl, const float2 *h, unsigned nb, unsigned P,
-                             unsigned *counter, unsigned *done, float s, int sms, cudaStream_t st)
+cudaError_t launch_upols_mac(float2 *y, const float2 *xcur, float2 *fdl, const float2 *h, float2 *part, unsigned nb,
+                             unsigned P, unsigned G, unsigned *tickets, float s, cudaStream_t st)
 {
-    unsigned blocks = (nb + 255) / 256;
-    const unsigned cap = 4u * (unsigned)(sms > 0 ? sms : 152);
-    blocks = blocks > cap ? cap : (blocks ? blocks : 1);
-    upols_mac<<<blocks, 256, 0, st>>>(y, xcur, fdl, h, nb, P, counter, done, s);
+    const unsigned gx = (nb + 255) / 256;
+    upols_mac<<<dim3(gx, G), 256, 0, st>>>(y, xcur, fdl, h, part, nb, P, tickets, s);
     return cudaGetLastError();
+}
+
+unsigned upols_chunks(unsigned nb, unsigned P, int sms)
+{
+    const unsigned gx = (nb + 255) / 256;
+    const unsigned want = 4u * (unsigned)(sms > 0 ? sms : 152);
+    unsigned G = (want + gx - 1) / gx;
+    return G < 1 ? 1 : (G > P ? P : G);
 }
 
 cudaError_t launch_fill_u32(unsigned *p, unsigned v, unsigned long long n, cudaStream_t st)
