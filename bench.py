@@ -222,8 +222,10 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
     algo_bytes_pass = 16.0 * N * B  # each pass reads and writes every point once (complex64)
 
     # schedule: measured choice (plan-time autotuning, outside the timed region)
-    tuned = lib.gb_autotune_1d(0, N, -1, 0, B, None, 0) == 0
-    plan = lib.gb_create_plan_1d_c2c_batched(N, -1, 0, B, 0, 0)
+    from mufft_gb300 import capi as K
+    pflags = {"none": 0, "bf16x3": K.FLAG_SPLIT_BF16X3, "bf16x2": K.FLAG_SPLIT_BF16X2}[args.split]
+    tuned = pflags == 0 and lib.gb_autotune_1d(0, N, -1, 0, B, None, 0) == 0
+    plan = lib.gb_create_plan_1d_c2c_batched(N, -1, pflags, B, 0, 0)
     if not plan:
         raise RuntimeError(lib.gb_last_error_string().decode())
     launches = lib.gb_plan_1d_launches(plan)
@@ -295,10 +297,10 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
     e2e = None
     if rank == 0 or world > 1:
         nbytes = elems * 8
-        if B == 1:
+        if B == 1 and not pflags:
             hplan = lib.create_plan_1d_c2c(N, -1, 0)
         else:
-            hplan = lib.gb_create_plan_1d_c2c_batched(N, -1, 0, B, 0, 0)
+            hplan = lib.gb_create_plan_1d_c2c_batched(N, -1, pflags, B, 0, 0)
         hin, hout = lib.alloc(nbytes), lib.alloc(nbytes)
         ctypes.memmove(hin, x.ctypes.data, nbytes)
         e2e_steps = max(3, min(args.steps, 10))
@@ -331,9 +333,10 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32" if not pflags else f"f32 via {args.split} tensor-core limbs",
         "data": "synthetic: complex64, re/im i.i.d. uniform [-1,1), SplitMix64 seed 2",
-        "config": {"workload": desc, "N": N, "batch": B, "parallelism": f"replicas x{world}",
+        "config": {"workload": desc + ("" if not pflags else f" [{args.split} split precision]"), "N": N, "batch": B,
+                   "parallelism": f"replicas x{world}",
                    "l2": f"inputs larger than L2: {nsets} rotating input/output sets of {16 * elems / 2**20:.0f} MiB",
                    "schedule": kernels,
                    "schedule_choice": "autotuned at plan time (mufft_gb_autotune_1d)" if tuned else "default heuristic"},
@@ -681,6 +684,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c_2^24")
     ap.add_argument("--batch", type=int, default=0, help="override the workload's batch (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--split", choices=["none", "bf16x3", "bf16x2"], default="none",
+                    help="run the workload's plan in split precision on the tensor cores (N = 256 or 4096)")
     ap.add_argument("--no-companions", action="store_true",
                     help="skip the split-precision, ragged-convolution and adjoint measurements")
     args = ap.parse_args()
