@@ -74,5 +74,27 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     return LIB
 
 
+CLI_SRC = PKG / "cli" / "mufft_bench.c"
+CLI = PKG / "mufft-bench"
+
+
+def build_cli() -> Path:
+    """The muFFT-style command-line benchmark (plain C against the library)."""
+    lib = build()
+    deps = [CLI_SRC, lib, *INCLUDE.glob("*.h")]
+    if CLI.exists() and CLI.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return CLI
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler for the command-line benchmark")
+    cmd = [cc, "-O2", "-std=c11", "-D_POSIX_C_SOURCE=200809L", f"-I{INCLUDE}", str(CLI_SRC), "-o", str(CLI),
+           f"-L{PKG}", "-lmufft_gb300", f"-Wl,-rpath,{PKG}", "-ldl", "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"mufft-bench build failed:\n{res.stdout}\n{res.stderr[:4000]}")
+    return CLI
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
+    print(build_cli())
