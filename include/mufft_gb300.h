@@ -254,6 +254,11 @@ int mufft_gb_autotune_save(const char *path);
 int mufft_gb_autotune_load(const char *path);
 void mufft_gb_autotune_clear(void);
 
+/* Column passes of multi-pass plans created afterwards stage each tile
+ * through a TMA tensor copy into shared memory, double-buffered in
+ * persistent CTAs (1) or single-buffered (2), or load it with per-thread
+ * loads (0, default). */
+int mufft_gb_set_tma(int mode);
 /* Split-precision plans (MUFFT_GB_FLAG_SPLIT_*) created afterwards run their
  * products on tcgen05.mma with TMEM accumulators (0, default) or on
  * warp-level mma.sync (1). */

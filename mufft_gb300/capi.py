@@ -91,6 +91,7 @@ GB_H = [
     ("conv_adjoint_input", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
     ("set_split_engine", _i, [_i]),
+    ("set_tma", _i, [_i]),
     ("autotune_1d", _i, [_i, _u, _i, _u, _u, _vp, _sz]),
     ("autotune_save", _i, [C.c_char_p]),
     ("autotune_load", _i, [C.c_char_p]),

@@ -14,6 +14,7 @@
 // Executes enqueue those launches on a stream.  The fft.h executes stage host
 // buffers through plan-owned device memory and synchronise before returning,
 // like the reference's synchronous calls (fft.c:811-989).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -35,6 +36,7 @@
 #include "conv_ragged.h"
 #include "misc_kernels.h"
 #include "split_tc.h"
+#include "tiles_tma.h"
 #include "registry.h"
 
 using namespace mgb;
@@ -111,13 +113,31 @@ static std::vector<TileKernel> &tile_table()
     return t;
 }
 
+static std::vector<TmaTileKernel> &tma_table()
+{
+    static std::vector<TmaTileKernel> t = [] {
+        std::vector<TmaTileKernel> v;
+        register_tiles_tma(v);
+        return v;
+    }();
+    return t;
+}
+
+static const TmaTileKernel *find_tma(int L, int R, int C, int nbuf)
+{
+    for (const TmaTileKernel &k : tma_table())
+        if (k.L == L && k.R == R && k.C == C && k.nbuf == nbuf)
+            return &k;
+    return nullptr;
+}
+
 static std::mutex g_choice_mu;
 static std::vector<TileKernel> g_choice;  // preferred (L, lmap, smap) -> C
 
 // Schedule choices of one plan (the autotuner's unit): -2 leaves a knob at its
 // process-wide setting; `tiles` are preferred (L, lmap, smap) -> (C, R, Q).
 struct PlanOptions {
-    int levels = -2, twiddle = -2, fused = -2;
+    int levels = -2, twiddle = -2, fused = -2, tma = -2;
     std::vector<TileKernel> tiles;
 };
 // Set while a plan is built with explicit choices (candidate or remembered).
@@ -225,6 +245,10 @@ bool device_prepare(int *dev_out)
         if (!cuda_ok(cudaMemcpy(ds.tw, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice),
                      "cudaMemcpy(twiddles)"))
             return false;
+        for (const TmaTileKernel &k : tma_table())
+            if (!cuda_ok(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem),
+                         "cudaFuncSetAttribute(tma)"))
+                return false;
         for (const TileKernel &k : tile_table()) {
             if (k.smem > 48 * 1024) {
                 if (!cuda_ok(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -294,6 +318,11 @@ struct Pass {
     BcArgs bc{};
     size_t bc_counter_bytes = 0;
     unsigned bc_grid = 0;
+    // column tile with TMA-staged input (tiles_tma.cu), used when the input
+    // layout allows it at launch; `k` is the fallback
+    const TmaTileKernel *tk = nullptr;
+    unsigned tma_grid = 0;
+    int *tma_err = nullptr;
     // split-precision tensor-core transform (split_tc.cu, split_umma.cu)
     SplitArgs sp{};
     int sp_stages = 0, sp_limbs = 0, sp_engine = 0;
@@ -318,6 +347,54 @@ const void *pick(Role r, const Buffers &b)
     }
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return (EncodeTiledFn)f;
+    }();
+    return fn;
+}
+
+// Tensor map of a column pass's input: {columns, L rows, row blocks} of
+// 8-byte elements, box {C, L, 1}.  False when the layout does not fit TMA's
+// rules (16-byte aligned base and strides, unit column distance, plain
+// prologue, uniform block stride); the pass then runs its regular kernel.
+bool tma_map_for(const Pass &p, const float2 *in, CUtensorMap *map)
+{
+    const TileArgs &a = p.a;
+    if (a.prologue != PRO_PLAIN || a.in_dist != 1 || ((uintptr_t)in & 15) || (a.in_stride & 1) || a.in_stride <= 0)
+        return false;
+    long long bstride = a.in_batch;
+    if (a.ysplit && a.in_batch2 != (long long)a.ysplit * a.in_batch)
+        return false;
+    if (p.grid.y <= 1)
+        bstride = a.in_stride * p.tk->L;
+    if (bstride & 1 || bstride < a.in_stride * p.tk->L)
+        return false;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc)
+        return false;
+    const cuuint64_t dims[3] = {a.ntrans, (cuuint64_t)p.tk->L, p.grid.y > 0 ? p.grid.y : 1};
+    const cuuint64_t strides[2] = {(cuuint64_t)a.in_stride * 8, (cuuint64_t)bstride * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)p.tk->C, (cuuint32_t)p.tk->L, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, (void *)in, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream_t st, size_t first = 0,
                        size_t count = (size_t)-1)
 {
@@ -330,6 +407,20 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             a.in = (const float2 *)pick(p.in_role, b);
             a.out = (float2 *)pick(p.out_role, b);
             a.in2 = (const float2 *)pick(p.in2_role, b);
+            if (p.tk) {
+                CUtensorMap map;
+                if (tma_map_for(p, a.in, &map)) {
+                    const unsigned tiles_x = (a.ntrans + p.tk->C - 1) / p.tk->C;
+                    unsigned ntiles = tiles_x * p.grid.y;
+                    int *err = p.tma_err;
+                    void *targs[] = {&map, &a, (void *)&tiles_x, &ntiles, &err};
+                    const unsigned grid = std::min(ntiles, p.tma_grid);
+                    cudaError_t e = cudaLaunchKernel(p.tk->fn, dim3(grid), dim3(p.tk->threads), targs, p.tk->smem, st);
+                    if (e != cudaSuccess)
+                        return e;
+                    continue;
+                }
+            }
             void *args[] = {&a};
             const size_t smem = (a.tw_lo || a.tw_colpow) ? p.k->smem : p.k->smem_ex;
             cudaError_t e;
@@ -405,8 +496,8 @@ std::string describe(const std::vector<Pass> &ps)
     for (size_t i = 0; i < ps.size(); i++) {
         const Pass &p = ps[i];
         if (p.type == PASS_TILE)
-            snprintf(buf, sizeof(buf), "%stile L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s%s conj=%d",
-                     i ? "; " : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
+            snprintf(buf, sizeof(buf), "%stile%s L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s%s conj=%d",
+                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
                      p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
@@ -491,6 +582,12 @@ std::atomic<int> g_fused_bc{0};
 // Split-precision products on tcgen05.mma (0, default) or warp-level mma.sync (1).
 std::atomic<int> g_split_engine{0};
 
+// Column passes with TMA-staged inputs: 1 double-buffered, 2 single buffer,
+// 0 off (default: on GB300 the staged 256-point column tiles run at two CTAs
+// per SM and measured 2 % (double-buffered) to 47 % (single) slower than the
+// per-thread loads at four CTAs per SM; the autotuner still tries them).
+std::atomic<int> g_tma{0};
+int opt_tma() { return (t_opts && t_opts->tma != -2) ? t_opts->tma : g_tma.load(); }
 int opt_twiddle() { return (t_opts && t_opts->twiddle != -2) ? t_opts->twiddle : g_twiddle_table.load(); }
 int opt_levels() { return (t_opts && t_opts->levels != -2) ? t_opts->levels : g_levels.load(); }
 int opt_fused() { return (t_opts && t_opts->fused != -2) ? t_opts->fused : g_fused_bc.load(); }
@@ -542,6 +639,39 @@ Pass column_pass(const TileKernel *k, const float2 *tw, unsigned L, unsigned nco
     p.a.scale = 1.0f;
     (void)L;
     return p;
+}
+
+// Gives every column pass whose tile has a TMA-staged variant that variant
+// (persistent grid: SMs x resident CTAs); the regular kernel stays as the
+// fallback for layouts TMA cannot describe.
+bool attach_tma(std::vector<Pass> &ps, PlanResources &res, bool dry, int device)
+{
+    const int mode = opt_tma();
+    if (mode == 0)
+        return true;
+    for (Pass &p : ps) {
+        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.k->lmap != ACROSS || p.k->smap != ACROSS)
+            continue;
+        const TmaTileKernel *tk = find_tma(p.k->L, p.k->R, p.k->C, mode == 2 ? 1 : 2);
+        if (!tk)
+            continue;
+        p.tk = tk;
+        if (dry) {
+            p.tma_grid = 2 * 152;
+            continue;
+        }
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tk->fn, tk->threads, tk->smem),
+                     "occupancy(tma)"))
+            return false;
+        p.tma_grid = (unsigned)(sms * std::max(per_sm, 1));
+        if (!res.err && (!cuda_ok(cudaMalloc(&res.err, sizeof(int)), "cudaMalloc(err)") ||
+                         !cuda_ok(cudaMemset(res.err, 0, sizeof(int)), "cudaMemset(err)")))
+            return false;
+        p.tma_err = res.err;
+    }
+    return true;
 }
 
 bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bool dry,
@@ -1141,7 +1271,8 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
             if (have)
                 t_opts = &tuned;
         }
-        const bool built = build_fft_passes(s, tw, pl->res, dry, pl->passes);
+        const bool built = build_fft_passes(s, tw, pl->res, dry, pl->passes) &&
+                           attach_tma(pl->passes, pl->res, dry, pl->device);
         t_opts = prev;
         if (!built) {
             destroy_1d(pl);
@@ -1215,7 +1346,7 @@ std::string describe_options(const PlanOptions &o)
 {
     std::string d;
     char b[160];
-    snprintf(b, sizeof(b), "levels=%d twiddle=%d fused=%d", o.levels, o.twiddle, o.fused);
+    snprintf(b, sizeof(b), "levels=%d twiddle=%d fused=%d tma=%d", o.levels, o.twiddle, o.fused, o.tma);
     d = b;
     for (const TileKernel &k : o.tiles) {
         snprintf(b, sizeof(b), " tile(L=%d %s/%s C=%d R=%d Q=%d)", k.L, k.lmap ? "across" : "along",
@@ -1336,6 +1467,15 @@ bool autotune_run(int kind, unsigned N, int direction, unsigned flags, unsigned 
                         cur_ms = t;
                     }
                 }
+        for (int tm = 0; tm <= 2; tm++) {
+            PlanOptions o = cur;
+            o.tma = tm;
+            const double t = measure(o, nullptr);
+            if (t < cur_ms) {
+                cur = o;
+                cur_ms = t;
+            }
+        }
         std::vector<TileKernel> roles;
         measure(cur, &roles);
         for (const TileKernel &role : roles) {
@@ -2537,13 +2677,13 @@ int mufft_gb_autotune_save(const char *path)
         set_error(MUFFT_GB_ERR_INVALID, "cannot write %s", path);
         return MUFFT_GB_ERR_INVALID;
     }
-    fprintf(f, "mufft_gb300-autotune 1\ndevice %d %s\n", sms, name.c_str());
+    fprintf(f, "mufft_gb300-autotune 2\ndevice %d %s\n", sms, name.c_str());
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         for (const auto &kv : g_tune) {
             const PlanOptions &o = kv.second;
-            fprintf(f, "entry %d %u %u %u %d %d %d %zu", kv.first.kind, kv.first.N, kv.first.batch, kv.first.flags,
-                    o.levels, o.twiddle, o.fused, o.tiles.size());
+            fprintf(f, "entry %d %u %u %u %d %d %d %d %zu", kv.first.kind, kv.first.N, kv.first.batch, kv.first.flags,
+                    o.levels, o.twiddle, o.fused, o.tma, o.tiles.size());
             for (const TileKernel &k : o.tiles)
                 fprintf(f, " %d %d %d %d %d %d", k.L, k.lmap, k.smap, k.C, k.R, k.Q);
             fprintf(f, "\n");
@@ -2573,7 +2713,7 @@ int mufft_gb_autotune_load(const char *path)
     }
     char line[4096], fname[256];
     int fsms = -1, version = 0;
-    bool ok = fgets(line, sizeof(line), f) && sscanf(line, "mufft_gb300-autotune %d", &version) == 1 && version == 1 &&
+    bool ok = fgets(line, sizeof(line), f) && sscanf(line, "mufft_gb300-autotune %d", &version) == 1 && version == 2 &&
               fgets(line, sizeof(line), f) && sscanf(line, "device %d %255s", &fsms, fname) == 2;
     if (!ok) {
         fclose(f);
@@ -2595,8 +2735,8 @@ int mufft_gb_autotune_load(const char *path)
         PlanOptions o;
         size_t nt = 0;
         int used = 0;
-        if (sscanf(line, "entry %d %u %u %u %d %d %d %zu%n", &k.kind, &k.N, &k.batch, &k.flags, &o.levels,
-                   &o.twiddle, &o.fused, &nt, &used) != 8 || nt > 16)
+        if (sscanf(line, "entry %d %u %u %u %d %d %d %d %zu%n", &k.kind, &k.N, &k.batch, &k.flags, &o.levels,
+                   &o.twiddle, &o.fused, &o.tma, &nt, &used) != 9 || nt > 16)
             continue;
         const char *q = line + used;
         bool good = true;
@@ -2616,6 +2756,16 @@ int mufft_gb_autotune_load(const char *path)
     std::lock_guard<std::mutex> lock(g_tune_mu);
     for (const auto &kv : loaded)
         g_tune[kv.first] = kv.second;
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_tma(int mode)
+{
+    if (mode < 0 || mode > 2) {
+        set_error(MUFFT_GB_ERR_INVALID, "mode must be 0 (off), 1 (double-buffered) or 2 (single buffer)");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_tma.store(mode);
     return MUFFT_GB_OK;
 }
 

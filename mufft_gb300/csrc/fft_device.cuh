@@ -434,6 +434,34 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
     }
 }
 
+// Stage-0 inputs of a column tile already staged in shared memory (by TMA):
+// element n of the tile's column c at sin[n*C + c].  Plain prologue only.
+template <int L, int R, int C>
+__device__ __forceinline__ void load_stage0_sin(const TileArgs &a, const float2 *sin, unsigned tr, int c, int tl,
+                                                float2 (&v)[R])
+{
+    using S = Sched<L, R>;
+    using TT = Tile<L, R, 1>;
+    constexpr int r = S::radix(0), NB = R / r, B = TT::B(0), TL = TT::TL;
+#pragma unroll
+    for (int q = 0; q < R; q++)
+        v[q] = make_float2(0.f, 0.f);
+    if (tr >= a.ntrans)
+        return;
+    const int mlim = a.half ? r / 2 : r;
+#pragma unroll
+    for (int u = 0; u < NB; u++)
+#pragma unroll
+        for (int m = 0; m < r; m++)
+            if (m < mlim)
+                v[u * r + m] = sin[(tl + TL * u + m * B) * C + c];
+    if (a.conj & 1) {
+#pragma unroll
+        for (int q = 0; q < R; q++)
+            v[q].y = -v[q].y;
+    }
+}
+
 // W_N^m = exp(-2*pi*i*m/N) for N <= 2^28 a power of two, scale = 2/N; m is
 // reduced mod N.  sincospif gets an exactly representable argument: m itself
 // when m < 2^24, otherwise the product of the twiddles of m's high and low
@@ -533,9 +561,9 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // transforms tile*C .. tile*C + C - 1; ioff / ooff shift the input / output
 // base (batches); j is the CTA's rank in its cluster.  COH: load with
 // L2-coherent loads (input written earlier in the same launch).
-template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH>
+template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
-                                          float2 *smem)
+                                          float2 *smem, const float2 *sin = nullptr)
 {
     using S = Sched<L, R>;
     using TT = Tile<L, R, Q>;
@@ -576,7 +604,12 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     float2 v[R];
     int c, tl;
     split_tid<LMAP, C, TL>(threadIdx.x, c, tl);
-    load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
+    if constexpr (SIN) {
+        static_assert(Q == 1 && LMAP == ACROSS, "staged inputs are column tiles");
+        load_stage0_sin<L, R, C>(a, sin, tile0 + c, c, tl, v);
+    } else {
+        load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
+    }
     stage_compute<L, R, Q, 0>(v, j, tl, a.tw);
     run_stages<L, R, C, Q, LMAP, SMAP, 1>(v, j, c, tl, smem, a.tw);
     // No CTA of the cluster may leave while others still read its slice.

@@ -192,3 +192,32 @@ def test_multipass_variants(gpu, torch, levels, fused, table, N, B):
         gpu.gb_set_multipass_levels(0)
         gpu.gb_set_fused_passes(0)
         gpu.gb_set_twiddle_table(-1)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("N,B", [(1 << 17, 3), (1 << 22, 1), (1 << 24, 1)])
+def test_tma_staged_column_passes(gpu, torch, mode, N, B):
+    """Column tiles staged by TMA tensor copies (double- and single-buffered
+    persistent CTAs) against FP64, both directions."""
+    x = signals.complex_uniform(26000 + N + B, N * B).reshape(B, N)
+    dx = _dev(torch, x)
+    dy = torch.empty_like(dx)
+    try:
+        assert gpu.gb_set_tma(mode) == 0
+        for direction in (K.FORWARD, K.INVERSE):
+            plan = gpu.gb_create_plan_1d_c2c_batched(N, direction, 0, B, 0, 0)
+            assert plan, gpu.gb_last_error_string()
+            buf = C.create_string_buffer(4096)
+            gpu.gb_plan_1d_describe(plan, buf, 4096)
+            assert b"+tma" in buf.value, buf.value
+            assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
+            torch.cuda.synchronize()
+            gpu.free_plan_1d(plan)
+            got = dy.cpu().numpy()
+            for r in range(B):
+                ref = np.fft.fft(x[r].astype(np.complex128))
+                if direction == K.INVERSE:
+                    ref = np.fft.ifft(x[r].astype(np.complex128)) * N
+                assert rel_l2(got[r], ref) < 2e-6, (r, direction)
+    finally:
+        gpu.gb_set_tma(0)
