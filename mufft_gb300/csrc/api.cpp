@@ -1477,7 +1477,7 @@ bool autotune_run(int kind, unsigned N, int direction, unsigned flags, unsigned 
             }
         }
         std::vector<TileKernel> roles;
-        measure(cur, &roles);
+        cur_ms = std::min(cur_ms, measure(cur, &roles));
         for (const TileKernel &role : roles) {
             for (const TileKernel &k : tile_table()) {
                 if (k.L != role.L || k.lmap != role.lmap || k.smap != role.smap)

@@ -1,7 +1,8 @@
 // Split-precision FFT stages on the 5th-generation tensor cores (tcgen05).
 //
 // Same mathematics as split_tc.cu (radix-16 Stockham stages of N = 256 / 4096
-// as Y = F16 X with BF16 limbs and FP32 accumulation), laid out for
+// as Y = F16 X with BF16 limbs and FP32 accumulation; here three limbs of X
+// are cut by truncation, so they represent X exactly), laid out for
 // tcgen05.mma: per stage the 256 DFT columns of a CTA's 4096 points form the
 // M dimension, so each product is
 //   D[j][n] += sum_kk A[j][kk] B[n][kk],   M = 128 columns j, N = 32, K = 32,
@@ -120,17 +121,34 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&d)[32])
         d[i] = __uint_as_float(r[i]);
 }
 
+// (a, b) as LIMBS bf16x2 pairs by truncation: each limb keeps the top 8
+// significant bits of what is left, the residual is exact, and three limbs
+// hold an FP32 value exactly (24 bits); two keep 16 bits.  The pair of high
+// halves is one byte permute.
+// Two limbs round to nearest instead (truncation would bias the 16 bits kept).
 template <int LIMBS>
 __device__ __forceinline__ void split2(float a, float b, unsigned (&o)[LIMBS])
 {
+    if constexpr (LIMBS == 3) {
+        unsigned ua = __float_as_uint(a), ub = __float_as_uint(b);
 #pragma unroll
-    for (int l = 0; l < LIMBS; l++) {
-        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-        memcpy(&o[l], &h, 4);
-        if (l + 1 < LIMBS) {
-            const float2 f = __bfloat1622float2(h);
-            a -= f.x;
-            b -= f.y;
+        for (int l = 0; l < LIMBS; l++) {
+            o[l] = __byte_perm(ua, ub, 0x7632);  // high half of a (low), high half of b (high)
+            if (l + 1 < LIMBS) {
+                ua = __float_as_uint(__uint_as_float(ua) - __uint_as_float(ua & 0xFFFF0000u));
+                ub = __float_as_uint(__uint_as_float(ub) - __uint_as_float(ub & 0xFFFF0000u));
+            }
+        }
+    } else {
+#pragma unroll
+        for (int l = 0; l < LIMBS; l++) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+            memcpy(&o[l], &h, 4);
+            if (l + 1 < LIMBS) {
+                const float2 f = __bfloat1622float2(h);
+                a -= f.x;
+                b -= f.y;
+            }
         }
     }
 }
@@ -238,8 +256,9 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
                         }
                 umma_commit(bar);
             }
-            // every thread waits for the commit; the outcome is made CTA-uniform
-            ok = __syncthreads_and(bar_wait(bar, phase & 1)) != 0;
+            // one thread waits for the commit (the others block in the barrier
+            // without issuing); the outcome is made CTA-uniform
+            ok = __syncthreads_and(tid == 0 ? bar_wait(bar, phase & 1) : true) != 0;
             if (!ok) {
                 if (tid == 0 && a.err)
                     atomicExch(a.err, 1);

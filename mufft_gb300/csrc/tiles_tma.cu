@@ -137,7 +137,9 @@ void register_tiles_tma(std::vector<TmaTileKernel> &out)
     TMA_TILE(256, 16, 16, 2);
     TMA_TILE(256, 16, 16, 1);
     TMA_TILE(128, 16, 32, 2);
+    TMA_TILE(128, 16, 32, 1);
     TMA_TILE(64, 16, 64, 2);
+    TMA_TILE(64, 16, 64, 1);
 #undef TMA_TILE
 }
 

@@ -58,7 +58,7 @@ def test_autotune_picks_a_correct_schedule(gpu, torch, N, B):
     assert len(lines) >= 3 and lines[-1].startswith("best")
     best_ms = float(lines[-1].split()[1])
     times = [float(l.split()[0]) for l in lines[:-1]]
-    assert best_ms <= min(times) + 1e-9
+    assert best_ms <= min(times) * 1.0001 + 1e-9, (best_ms, min(times))
     tuned = describe(gpu, N, batch=B)
     assert run_c2c(gpu, torch, N, B) < 2e-6, (default, tuned)
 
