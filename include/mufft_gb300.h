@@ -140,11 +140,23 @@ typedef struct mufft_gb_conv_request {
 
 typedef struct mufft_gb_conv_batch mufft_gb_conv_batch;
 
-/* Prepares `count` requests of mixed sizes for one persistent launch (requests
- * ordered longest first, each run by one CTA), captured in a CUDA graph.
- * flags: 0. */
+/* Prepares `count` requests of mixed sizes for one persistent launch,
+ * captured in a CUDA graph.  Requests are ordered longest first; those of at
+ * least the split size (2^16 complex points by default) run as phase tasks
+ * spread over many CTAs, the others whole in one CTA each.  flags: 0, or
+ * MUFFT_GB_FLAG_AUTOTUNE to time the batch with every split size (running
+ * it, so writing the outputs, a few times) and keep the fastest. */
 mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *requests, unsigned count,
                                                 unsigned flags);
+/* Default split size of batches created afterwards: a power of two in
+ * 16384..65536 complex points, or 0 to run every request whole. */
+int mufft_gb_set_conv_split(unsigned points);
+/* The split size in use (complex points; 0: no request is split). */
+unsigned mufft_gb_conv_batch_split_size(const mufft_gb_conv_batch *batch);
+/* Synchronises the device and reports whether a bounded wait of the batch's
+ * task dependencies timed out in an earlier execute (MUFFT_GB_ERR_UNSUPPORTED),
+ * clearing the flag. */
+int mufft_gb_conv_batch_status(mufft_gb_conv_batch *batch);
 /* Replays the batch on `stream` (enqueued, not synchronised).  Executes of one
  * batch must not overlap on the GPU (they share its scratch). */
 int mufft_gb_execute_conv_batch(mufft_gb_conv_batch *batch, void *stream);

@@ -1924,13 +1924,19 @@ struct mufft_gb_conv_batch {
     int device = -1;
     unsigned count = 0;
     RaggedReq *d_reqs = nullptr;
-    unsigned *d_next = nullptr;
+    RaggedTask *d_tasks = nullptr;
+    unsigned *d_next = nullptr;      // [0] dequeue counter, [1..] per split request completed tasks
+    int *d_err = nullptr;
     float2 *d_scratch = nullptr;
     float2 *d_rtw = nullptr;
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned grid = 0;
+    unsigned split_lg = 16;          // requests of 2^split_lg complex points and more run as phase tasks
+    std::vector<RaggedReq> sorted;   // longest first (host copy)
+    RaggedArgs args{};
+    size_t smem = 0;
 };
 
 namespace {
@@ -1948,11 +1954,95 @@ void destroy_conv_batch(mufft_gb_conv_batch *b)
         if (b->capture)
             cudaStreamDestroy(b->capture);
         cudaFree(b->d_reqs);
+        cudaFree(b->d_tasks);
+        cudaFree(b->d_err);
         cudaFree(b->d_next);
         cudaFree(b->d_scratch);
         cudaFree(b->d_rtw);
     }
     delete b;
+}
+
+// Split size of ragged batches created afterwards (log2 of complex points;
+// 17: no request is split), set with mufft_gb_set_conv_split.  Default 2^16:
+// on the 512-request mix (2^8..2^16 points) splitting the 65536-point
+// requests took the batch from 0.19 to 0.177 ms, splitting 32768 and 16384
+// as well cost more in task overhead than it gained (0.226, 0.259 ms).
+std::atomic<unsigned> g_conv_split_lg{16};
+
+// Task list for a split size, uploaded with the request table, and the graph
+// (counter resets + the persistent launch) that replays it.
+bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg)
+{
+    DeviceGuard g(b->device);
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaFree(b->d_tasks);
+    cudaFree(b->d_next);
+    b->d_tasks = nullptr;
+    b->d_next = nullptr;
+    b->split_lg = split_lg;
+    std::vector<RaggedReq> reqs = b->sorted;
+    std::vector<unsigned> split_ids, whole_ids;
+    unsigned nsplit = 0;
+    for (unsigned i = 0; i < reqs.size(); i++) {
+        reqs[i].split = reqs[i].lg >= split_lg && reqs[i].lg >= kRaggedMinSplitLg ? 1 : 0;
+        if (reqs[i].split) {
+            reqs[i].counter = 1 + nsplit++;
+            split_ids.push_back(i);
+        } else {
+            whole_ids.push_back(i);
+        }
+    }
+    // phase-major over split requests, with whole requests (longest first) in between
+    std::vector<RaggedTask> tasks;
+    size_t w = 0;
+    for (unsigned phase = 0; phase < 5; phase++) {
+        for (unsigned r : split_ids) {
+            unsigned before = 0;
+            for (unsigned p = 0; p < phase; p++)
+                before += ragged_phase_tasks(reqs[r].lg, p);
+            for (unsigned t = 0; t < ragged_phase_tasks(reqs[r].lg, phase); t++)
+                tasks.push_back(RaggedTask{r, (unsigned short)phase, (unsigned short)t, before, 0});
+        }
+        const size_t take = phase == 4 ? whole_ids.size() - w : (whole_ids.size() - w) / (5 - phase);
+        for (size_t k = 0; k < take; k++, w++)
+            tasks.push_back(RaggedTask{whole_ids[w], 0, 0, 0, 0});
+    }
+    b->args.count = (unsigned)tasks.size();
+    if (!cuda_ok(cudaMalloc(&b->d_tasks, tasks.size() * sizeof(RaggedTask)), "cudaMalloc(tasks)") ||
+        !cuda_ok(cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(RaggedTask), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(tasks)") ||
+        !cuda_ok(cudaMemcpy(b->d_reqs, reqs.data(), reqs.size() * sizeof(RaggedReq), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(requests)") ||
+        !cuda_ok(cudaMalloc(&b->d_next, (1 + nsplit) * sizeof(unsigned)), "cudaMalloc(counters)"))
+        return false;
+    b->args.tasks = b->d_tasks;
+    b->args.next = b->d_next;
+    b->args.counters = b->d_next;
+    b->args.err = b->d_err;
+    const unsigned grid = std::min<unsigned>(b->grid, (unsigned)tasks.size());
+    void *kargs[] = {&b->args};
+    bool ok = cuda_ok(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "capture") &&
+              cuda_ok(cudaMemsetAsync(b->d_next, 0, (1 + nsplit) * sizeof(unsigned), b->capture), "cudaMemsetAsync") &&
+              cuda_ok(cudaLaunchKernel(conv_ragged_fn(), dim3(grid), dim3(conv_ragged_threads()), kargs, b->smem,
+                                       b->capture),
+                      "kernel launch");
+    cudaGraph_t gr = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b->capture, &gr);
+    if (!ok || !cuda_ok(ce, "capture") || !cuda_ok(cudaGraphInstantiate(&b->exec, gr, 0), "cudaGraphInstantiate")) {
+        if (gr)
+            cudaGraphDestroy(gr);
+        return false;
+    }
+    b->graph = gr;
+    return true;
 }
 
 }  // namespace
@@ -1962,7 +2052,6 @@ extern "C" {
 mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *requests, unsigned count,
                                                 unsigned flags)
 {
-    (void)flags;
     t_err = 0;
     if (!requests || count == 0) {
         set_error(MUFFT_GB_ERR_INVALID, "no requests");
@@ -2005,7 +2094,7 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
     mufft_gb_conv_batch *b = new mufft_gb_conv_batch();
     b->device = dev;
     b->count = count;
-    RaggedArgs args{};
+    RaggedArgs &args = b->args;
     // per-size r2c / c2r fix-up twiddles, FP64 then rounded (fft.c:441-455)
     std::vector<float2> rtw;
     for (unsigned lg = 0; lg <= 16; lg++) {
@@ -2030,51 +2119,64 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
     for (unsigned i = 0; i < count; i++)
         order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](unsigned x, unsigned y) { return cost[x] > cost[y]; });
-    std::vector<RaggedReq> sorted(count);
+    b->sorted.resize(count);
     for (unsigned i = 0; i < count; i++) {
-        sorted[i] = reqs[order[i]];
-        sorted[i].spec = b->d_scratch + spec_off[order[i]];
+        b->sorted[i] = reqs[order[i]];
+        b->sorted[i].spec = b->d_scratch + spec_off[order[i]];
     }
-    if (!cuda_ok(cudaMemcpy(b->d_reqs, sorted.data(), count * sizeof(RaggedReq), cudaMemcpyHostToDevice),
-                 "cudaMemcpy(requests)")) {
-        destroy_conv_batch(b);
-        return nullptr;
-    }
-    const size_t smem = conv_ragged_smem();
+    b->smem = conv_ragged_smem();
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (!cuda_ok(cudaFuncSetAttribute(conv_ragged_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    if (!cuda_ok(cudaFuncSetAttribute(conv_ragged_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem),
                  "cudaFuncSetAttribute") ||
-        !cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_ragged_fn(), conv_ragged_threads(), smem),
-                 "occupancy")) {
+        !cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_ragged_fn(), conv_ragged_threads(),
+                                                               b->smem),
+                 "occupancy") ||
+        !cuda_ok(cudaMalloc(&b->d_err, sizeof(int)), "cudaMalloc(err)") ||
+        !cuda_ok(cudaMemset(b->d_err, 0, sizeof(int)), "cudaMemset(err)") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "cudaStreamCreate")) {
         destroy_conv_batch(b);
         return nullptr;
     }
     b->grid = (unsigned)(sms * std::max(per_sm, 1));
-    if (b->grid > count)
-        b->grid = count;
-    args.reqs = b->d_reqs;
-    args.count = count;
-    args.next = b->d_next;
-    args.tw = g_dev[dev].tw;
-    args.rtw = b->d_rtw;
-    // capture counter reset + the persistent launch once; executes replay the graph
-    void *kargs[] = {&args};
-    bool ok = cuda_ok(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "cudaStreamCreate") &&
-              cuda_ok(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "capture") &&
-              cuda_ok(cudaMemsetAsync(b->d_next, 0, sizeof(unsigned), b->capture), "cudaMemsetAsync") &&
-              cuda_ok(cudaLaunchKernel(conv_ragged_fn(), dim3(b->grid), dim3(conv_ragged_threads()), kargs, smem,
-                                       b->capture),
-                      "kernel launch");
-    cudaGraph_t g = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(b->capture, &g);
-    if (!ok || !cuda_ok(ce, "capture") || !cuda_ok(cudaGraphInstantiate(&b->exec, g, 0), "cudaGraphInstantiate")) {
-        if (g)
-            cudaGraphDestroy(g);
+    b->args.reqs = b->d_reqs;
+    b->args.tw = g_dev[dev].tw;
+    b->args.rtw = b->d_rtw;
+    unsigned best_lg = g_conv_split_lg.load();
+    if (flags & MUFFT_GB_FLAG_AUTOTUNE) {
+        // time the batch with every split size (17: nothing split) and keep the fastest
+        cudaEvent_t e0, e1;
+        double best = INFINITY;
+        bool ok = cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") && cuda_ok(cudaEventCreate(&e1), "cudaEventCreate");
+        for (unsigned lg = kRaggedMinSplitLg; ok && lg <= 17; lg++) {
+            if (!conv_batch_build(b, lg)) {
+                ok = false;
+                break;
+            }
+            for (int wu = 0; wu < 2; wu++)
+                cudaGraphLaunch(b->exec, b->capture);
+            cudaEventRecord(e0, b->capture);
+            for (int r = 0; r < 5; r++)
+                cudaGraphLaunch(b->exec, b->capture);
+            cudaEventRecord(e1, b->capture);
+            float ms = 0.f;
+            ok = cuda_ok(cudaEventSynchronize(e1), "autotune") && cuda_ok(cudaEventElapsedTime(&ms, e0, e1), "autotune");
+            if (ok && ms < best) {
+                best = ms;
+                best_lg = lg;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (!ok) {
+            destroy_conv_batch(b);
+            return nullptr;
+        }
+    }
+    if (!conv_batch_build(b, best_lg)) {
         destroy_conv_batch(b);
         return nullptr;
     }
-    b->graph = g;
     return b;
 }
 
@@ -2088,6 +2190,30 @@ int mufft_gb_execute_conv_batch(mufft_gb_conv_batch *batch, void *stream)
     if (!cuda_ok(cudaGraphLaunch(batch->exec, (cudaStream_t)stream), "cudaGraphLaunch"))
         return t_err;
     return MUFFT_GB_OK;
+}
+
+int mufft_gb_conv_batch_status(mufft_gb_conv_batch *batch)
+{
+    if (!batch) {
+        set_error(MUFFT_GB_ERR_INVALID, "null batch");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(batch->device);
+    int e = 0;
+    if (!cuda_ok(cudaDeviceSynchronize(), "synchronize") ||
+        !cuda_ok(cudaMemcpy(&e, batch->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag"))
+        return t_err;
+    if (e) {
+        cudaMemset(batch->d_err, 0, sizeof(int));
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "a bounded wait in the ragged batch timed out");
+        return MUFFT_GB_ERR_UNSUPPORTED;
+    }
+    return MUFFT_GB_OK;
+}
+
+unsigned mufft_gb_conv_batch_split_size(const mufft_gb_conv_batch *batch)
+{
+    return batch ? (batch->split_lg >= 17 ? 0u : 1u << batch->split_lg) : 0u;
 }
 
 void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch) { destroy_conv_batch(batch); }
@@ -2756,6 +2882,16 @@ int mufft_gb_autotune_load(const char *path)
     std::lock_guard<std::mutex> lock(g_tune_mu);
     for (const auto &kv : loaded)
         g_tune[kv.first] = kv.second;
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_conv_split(unsigned points)
+{
+    if (points != 0 && (!is_pow2(points) || points < (1u << kRaggedMinSplitLg) || points > 65536)) {
+        set_error(MUFFT_GB_ERR_INVALID, "split size must be 0 or a power of two in 16384..65536");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_conv_split_lg.store(points ? ilog2u(points) : 17u);
     return MUFFT_GB_OK;
 }
 

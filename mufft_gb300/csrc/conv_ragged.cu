@@ -8,8 +8,15 @@
 // goes through an N/2-point complex FFT with the r2c/c2r fix-ups,
 // STEREO_MONO through an N-point complex FFT (fft.c:585-599).
 //
-// Every CTA (512 threads) takes the next request from a global counter, the
-// host having sorted requests longest first, and runs it alone:
+// Every CTA (512 threads) takes the next work item from a global counter.
+// The host orders the items (longest requests first) and decides which
+// requests are split: a split request of L = L1 x L2 >= 16384 points runs as
+// five phases of tasks (F1 column tiles, F2 row tiles, multiply chunks, I1 row
+// tiles, I2 column tiles) that any CTA may take, each task waiting (bounded)
+// on a per-request counter until the previous phase is complete; phases are
+// queued phase-major across requests, so the waits are rarely long, and every
+// awaited task was dequeued earlier by a running CTA (no deadlock).  A request
+// that is not split runs whole in one CTA:
 //   L <= 8192 complex points: one forward tile (r2c fix-up fused into its
 //     store for mono) writes the spectrum to the request's scratch, which
 //     stays in L2; one inverse tile reads it back with the multiply and the
@@ -73,15 +80,18 @@ __device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, 
     __syncthreads();
 }
 
-// Multiply phase of the four-step path on the transposed spectrum.
+// Multiply phase of the four-step path on the transposed spectrum, for the
+// chunk `chunk` of `nchunks` (pairs k, L-k for mono; elements for stereo).
 template <int L1, int L2>
-__device__ void conv_multiply(const RaggedReq &q, const float2 *rtw_fwd, const float2 *rtw_inv)
+__device__ void conv_multiply(const RaggedReq &q, const float2 *rtw_fwd, const float2 *rtw_inv, unsigned chunk,
+                              unsigned nchunks)
 {
     constexpr int L = L1 * L2;
     float2 *s = q.spec;
     auto at = [](int k) { return (k % L1) * L2 + k / L1; };  // X[k] lives at X^T[k % L1][k / L1]
     if (q.stereo) {
-        for (int idx = threadIdx.x; idx < L; idx += kThreads) {
+        const int i0 = (int)((long long)L * chunk / nchunks), i1 = (int)((long long)L * (chunk + 1) / nchunks);
+        for (int idx = i0 + threadIdx.x; idx < i1; idx += kThreads) {
             const int k = (idx / L2) + L1 * (idx % L2);
             s[idx] = cscale(cmul(__ldcg(&s[idx]), __ldcg(&q.h[k])), q.scale);
         }
@@ -89,7 +99,9 @@ __device__ void conv_multiply(const RaggedReq &q, const float2 *rtw_fwd, const f
     }
     // mono: Z (forward complex FFT of the packed reals) -> r2c bins X -> Y = s*X*H
     // -> c2r pre-pass Zi, pair by pair (kernel.c:36-82).
-    for (int k = threadIdx.x; k <= L / 2; k += kThreads) {
+    constexpr int NP = L / 2 + 1;
+    const int k0 = (int)((long long)NP * chunk / nchunks), k1 = (int)((long long)NP * (chunk + 1) / nchunks);
+    for (int k = k0 + threadIdx.x; k < k1; k += kThreads) {
         if (k == 0) {
             const float2 z0 = __ldcg(&s[0]);
             const float2 x0 = make_float2(z0.x + z0.y, 0.f), xm = make_float2(z0.x - z0.y, 0.f);
@@ -112,63 +124,125 @@ __device__ void conv_multiply(const RaggedReq &q, const float2 *rtw_fwd, const f
     }
 }
 
+template <int L1, int L2> __host__ __device__ constexpr int c1_of() { return kThreads * 16 / L1; }
+template <int L1, int L2> __host__ __device__ constexpr int c2_of() { return kThreads * 16 / L2; }
+
+// Tile arguments of the four phases that transform (F1, F2, I1, I2).
 template <int L1, int L2>
-__device__ void conv_multi(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
-                           const float2 *rtw_inv)
+__device__ TileArgs multi_args(const RaggedReq &q, const float2 *tw, int phase)
 {
     constexpr int L = L1 * L2;
-    constexpr int C1 = kThreads * 16 / L1, C2 = kThreads * 16 / L2;
     TileArgs a{};
     a.tw = tw;
     a.scale = 1.0f;
     a.tw_scale = 2.0f / (float)L;
     a.tw_mask = L - 1;
+    if (phase == 0 || phase == 4) {
+        // columns of length L1 (n1), stride L2, twiddle W_L^(k1*n2) on the way in
+        a.in = phase == 0 ? q.in : q.spec;
+        a.out = phase == 0 ? q.spec : q.out;
+        a.in_stride = a.out_stride = L2;
+        a.in_dist = a.out_dist = 1;
+        a.ntrans = L2;
+        a.half = phase == 0 ? q.zero_pad : 0;
+        a.epilogue = phase == 0 ? EPI_TWIDDLE : EPI_PLAIN;
+        a.conj = phase == 0 ? 0 : 2;  // I2: inverse over k1 of conj(Z), conjugated out
+    } else {
+        // rows of length L2, in place; I1: inverse over k2 (conj in, forward FFT,
+        // W_L^(n2*k1)) -> conj(Z)
+        a.in = q.spec;
+        a.out = q.spec;
+        a.in_stride = a.out_stride = 1;
+        a.in_dist = a.out_dist = L2;
+        a.ntrans = L1;
+        a.conj = phase == 3 ? 1 : 0;
+        a.epilogue = phase == 3 ? EPI_TWIDDLE : EPI_PLAIN;
+    }
+    return a;
+}
 
-    // F1: columns of length L1 (n1), stride L2, twiddle W_L^(k1*n2)
-    TileArgs f1 = a;
-    f1.in = q.in;
-    f1.out = q.spec;
-    f1.in_stride = f1.out_stride = L2;
-    f1.in_dist = f1.out_dist = 1;
-    f1.ntrans = L2;
-    f1.half = q.zero_pad;
-    f1.epilogue = EPI_TWIDDLE;
-    for (int t = 0; t < L2 / C1; t++)
-        tile_body<L1, 16, C1, 1, ACROSS, ACROSS, false>(f1, t, 0, 0, 0, smem);
-    __syncthreads();
-    // F2: rows of length L2, in place -> X^T[k1][k2]
-    TileArgs f2 = a;
-    f2.in = q.spec;
-    f2.out = q.spec;
-    f2.in_stride = f2.out_stride = 1;
-    f2.in_dist = f2.out_dist = L2;
-    f2.ntrans = L1;
-    for (int t = 0; t < L1 / C2; t++)
-        tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(f2, t, 0, 0, 0, smem);
-    __syncthreads();
-    conv_multiply<L1, L2>(q, rtw_fwd, rtw_inv);
-    __syncthreads();
-    // I1: rows, inverse over k2: conj in, forward FFT, W_L^(n2*k1) -> conj(Z)
-    TileArgs i1 = f2;
-    i1.conj = 1;
-    i1.epilogue = EPI_TWIDDLE;
-    for (int t = 0; t < L1 / C2; t++)
-        tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(i1, t, 0, 0, 0, smem);
-    __syncthreads();
-    // I2: columns, inverse over k1 of conj(Z): forward FFT, conj out -> natural output
-    TileArgs i2 = a;
-    i2.in = q.spec;
-    i2.out = q.out;
-    i2.in_stride = i2.out_stride = L2;
-    i2.in_dist = i2.out_dist = 1;
-    i2.ntrans = L2;
-    i2.conj = 2;
-    for (int t = 0; t < L2 / C1; t++)
-        tile_body<L1, 16, C1, 1, ACROSS, ACROSS, true>(i2, t, 0, 0, 0, smem);
-    __syncthreads();
+// One phase task of a split request (or, with index < 0, the whole phase).
+template <int L1, int L2>
+__device__ void multi_phase(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
+                            const float2 *rtw_inv, int phase, int index)
+{
+    constexpr int C1 = c1_of<L1, L2>(), C2 = c2_of<L1, L2>();
+    if (phase == 2) {
+        if (index < 0)
+            conv_multiply<L1, L2>(q, rtw_fwd, rtw_inv, 0, 1);
+        else
+            conv_multiply<L1, L2>(q, rtw_fwd, rtw_inv, (unsigned)index, kRaggedMulChunks);
+        return;
+    }
+    const TileArgs a = multi_args<L1, L2>(q, tw, phase);
+    if (phase == 0 || phase == 4) {
+        const int t0 = index < 0 ? 0 : index, t1 = index < 0 ? L2 / C1 : index + 1;
+        for (int t = t0; t < t1; t++) {
+            if (phase == 0)
+                tile_body<L1, 16, C1, 1, ACROSS, ACROSS, false>(a, t, 0, 0, 0, smem);
+            else
+                tile_body<L1, 16, C1, 1, ACROSS, ACROSS, true>(a, t, 0, 0, 0, smem);
+            __syncthreads();
+        }
+    } else {
+        const int t0 = index < 0 ? 0 : index, t1 = index < 0 ? L1 / C2 : index + 1;
+        for (int t = t0; t < t1; t++) {
+            tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(a, t, 0, 0, 0, smem);
+            __syncthreads();
+        }
+    }
+}
+
+// Whole request through the in-CTA four-step.
+template <int L1, int L2>
+__device__ void conv_multi(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
+                           const float2 *rtw_inv)
+{
+    for (int phase = 0; phase < 5; phase++) {
+        multi_phase<L1, L2>(q, smem, tw, rtw_fwd, rtw_inv, phase, -1);
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Thread 0 waits (bounded) until *ctr >= target; CTA-uniform result.
+__device__ bool wait_tasks(const unsigned *ctr, unsigned target, int *err)
+{
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        for (unsigned i = 0; ld_acquire_u32(ctr) < target; i++) {
+            if (i > (1u << 24) || *(volatile int *)err) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(128);
+        }
+    }
+    return __syncthreads_and(ok) != 0;
 }
 
 }  // namespace
+
+unsigned ragged_phase_tasks(unsigned lg, unsigned phase)
+{
+    // four-step split L1 x L2 of the in-CTA path: 2^14 = 128 x 128, 2^15 = 128 x 256, 2^16 = 256 x 256
+    const unsigned l1 = lg == 16 ? 256 : 128, l2 = lg == 14 ? 128 : 256;
+    const unsigned c1 = kThreads * 16 / l1, c2 = kThreads * 16 / l2;
+    switch (phase) {
+    case 0:
+    case 4: return l2 / c1;
+    case 1:
+    case 3: return l1 / c2;
+    default: return kRaggedMulChunks;
+    }
+}
 
 __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedArgs args)
 {
@@ -182,9 +256,25 @@ __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedAr
         __syncthreads();
         if (i >= args.count)
             return;
-        const RaggedReq q = args.reqs[i];
+        const RaggedTask task = args.tasks[i];
+        const RaggedReq q = args.reqs[task.req];
         const float2 *rf = args.rtw + args.rtw_off[q.lg];
         const float2 *ri = rf + (1u << q.lg);
+        if (q.split) {
+            if (task.wait && !wait_tasks(&args.counters[q.counter], task.wait, args.err))
+                return;
+            switch (q.lg) {
+            case 14: multi_phase<128, 128>(q, smem, args.tw, rf, ri, task.phase, task.index); break;
+            case 15: multi_phase<128, 256>(q, smem, args.tw, rf, ri, task.phase, task.index); break;
+            case 16: multi_phase<256, 256>(q, smem, args.tw, rf, ri, task.phase, task.index); break;
+            default: break;
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+                atomicAdd(&args.counters[q.counter], 1u);
+            continue;
+        }
         switch (q.lg) {
         case 4: conv_single<16>(q, smem, args.tw, rf, ri); break;
         case 5: conv_single<32>(q, smem, args.tw, rf, ri); break;
@@ -221,7 +311,7 @@ size_t conv_ragged_smem()
     const size_t v[] = {single_bytes<16>(),   single_bytes<32>(),   single_bytes<64>(),   single_bytes<128>(),
                         single_bytes<256>(),  single_bytes<512>(),  single_bytes<1024>(), single_bytes<2048>(),
                         single_bytes<4096>(), single_bytes<8192>(), single_bytes<16384>(),
-                        multi_bytes<128, 256>(), multi_bytes<256, 256>()};
+                        multi_bytes<128, 128>(), multi_bytes<128, 256>(), multi_bytes<256, 256>()};
     size_t m = 0;
     for (size_t x : v)
         m = x > m ? x : m;

@@ -17,15 +17,34 @@ struct RaggedReq {
     unsigned lg;          // log2 of the complex FFT length L (mono N/2, stereo N)
     unsigned stereo;
     unsigned zero_pad;    // first block zero-padded (upper half not read)
+    unsigned split;       // 1: runs as phase tasks (four-step over several CTAs)
+    unsigned counter;     // split requests: index of its completion counter
 };
 
+// Work item: a whole request, or one task of a phase of a split request.
+struct RaggedTask {
+    unsigned req;
+    unsigned short phase;  // split: 0 F1 columns, 1 F2 rows, 2 multiply, 3 I1 rows, 4 I2 columns
+    unsigned short index;  // tile / chunk within the phase
+    unsigned wait;         // tasks of this request that must be complete first
+    unsigned pad;
+};
+
+// Phase task counts of a split request of length 2^lg (four-step L1 x L2).
+constexpr unsigned kRaggedMulChunks = 8;
+unsigned ragged_phase_tasks(unsigned lg, unsigned phase);
+constexpr unsigned kRaggedMinSplitLg = 14;  // split requests have L >= 16384
+
 struct RaggedArgs {
-    const RaggedReq *reqs;  // sorted longest first
-    unsigned count;
-    unsigned *next;         // dequeue counter, zeroed before each launch
-    const float2 *tw;       // stage twiddle table
-    const float2 *rtw;      // per size: r2c fix-up twiddles (L) then c2r ones (L)
-    unsigned rtw_off[17];   // offset of size 2^lg in rtw
+    const RaggedReq *reqs;
+    const RaggedTask *tasks;  // in dequeue order
+    unsigned count;           // tasks
+    unsigned *next;           // dequeue counter, zeroed before each launch
+    unsigned *counters;       // per split request: completed tasks, zeroed before each launch
+    int *err;                 // set when a bounded wait times out
+    const float2 *tw;         // stage twiddle table
+    const float2 *rtw;        // per size: r2c fix-up twiddles (L) then c2r ones (L)
+    unsigned rtw_off[17];     // offset of size 2^lg in rtw
 };
 
 const void *conv_ragged_fn();

@@ -57,7 +57,7 @@ def filter_spectrum(gpu, b: np.ndarray, N: int, method: int) -> np.ndarray:
 class Batch:
     """Device buffers and the batch handle for a list of (N, method) requests."""
 
-    def __init__(self, gpu, torch, specs, seed):
+    def __init__(self, gpu, torch, specs, seed, flags=0):
         self.gpu, self.specs = gpu, specs
         self.a, self.b, self.din, self.dh, self.dout = [], [], [], [], []
         reqs = (K.ConvRequest * len(specs))()
@@ -71,13 +71,14 @@ class Batch:
             dout = torch.full((N,), float("nan"), dtype=torch.complex64 if stereo else torch.float32, device="cuda")
             reqs[i] = K.ConvRequest(N, method, din.data_ptr(), dh.data_ptr(), dout.data_ptr())
             self.a.append(a), self.b.append(b), self.din.append(din), self.dh.append(dh), self.dout.append(dout)
-        self.handle = gpu.gb_create_conv_batch(reqs, len(specs), 0)
+        self.handle = gpu.gb_create_conv_batch(reqs, len(specs), flags)
         assert self.handle, gpu.gb_last_error_string()
 
     def run(self, torch):
         rc = self.gpu.gb_execute_conv_batch(self.handle, torch.cuda.current_stream().cuda_stream)
         assert rc == 0, self.gpu.gb_last_error_string()
         torch.cuda.synchronize()
+        assert self.gpu.gb_conv_batch_status(self.handle) == 0, self.gpu.gb_last_error_string()
         return [d.cpu().numpy() for d in self.dout]
 
     def free(self):
@@ -172,3 +173,40 @@ def test_conv_batch_rejects_bad_requests(gpu, torch):
         gpu.gb_clear_error()
     assert not gpu.gb_create_conv_batch(None, 0, 0)
     gpu.gb_clear_error()
+
+
+def test_conv_batch_autotuned_split_size(gpu, ora, torch):
+    """MUFFT_GB_FLAG_AUTOTUNE times every split size; whatever it keeps, the
+    outputs match the oracle (split and whole paths of every large size)."""
+    specs = [(1 << 17, 0), (1 << 16, STEREO), (1 << 15, PAD1), (1 << 15, STEREO | PAD1), (1 << 16, 0),
+             (1 << 14, STEREO)] + _mixed_specs(13, 40)
+    bt = Batch(gpu, torch, specs, 94000, flags=K.FLAG_AUTOTUNE)
+    try:
+        split = gpu.gb_conv_batch_split_size(bt.handle)
+        assert split in (0, 1 << 14, 1 << 15, 1 << 16)
+        outs = bt.run(torch)
+    finally:
+        bt.free()
+    for i, ((N, method), got) in enumerate(zip(specs, outs)):
+        want = ora.conv(bt.a[i], bt.b[i], N, method)
+        assert rel_l2(got, want) <= REL_L2_TOL, (i, N, method, split)
+
+
+@pytest.mark.parametrize("split", [0, 1 << 14, 1 << 15])
+def test_conv_batch_forced_split_sizes(gpu, ora, torch, split):
+    """Every split size gives the oracle's outputs (phase tasks with their
+    bounded dependency waits, or whole requests)."""
+    specs = [(1 << 17, 0), (1 << 16, STEREO), (1 << 15, PAD1), (1 << 15, STEREO | PAD1), (1 << 16, PAD1 | PAD2),
+             (1 << 14, STEREO), (2048, 0), (64, STEREO)]
+    try:
+        assert gpu.gb_set_conv_split(split) == 0
+        bt = Batch(gpu, torch, specs, 95000 + split)
+    finally:
+        gpu.gb_set_conv_split(1 << 16)
+    try:
+        assert gpu.gb_conv_batch_split_size(bt.handle) == split
+        outs = bt.run(torch)
+    finally:
+        bt.free()
+    for i, ((N, method), got) in enumerate(zip(specs, outs)):
+        assert rel_l2(got, ora.conv(bt.a[i], bt.b[i], N, method)) <= REL_L2_TOL, (i, N, method, split)
