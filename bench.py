@@ -358,12 +358,10 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
     if world == 1 and not args.no_companions:
         del ins, outs
         torch.cuda.empty_cache()
-        res["batched_1024"] = companion_batched_1024(lib, torch)
-        res["fft2d_4096"] = companion_2d(lib, torch)
-        res["split_tc"] = companion_split(lib, torch)
-        res["ragged_conv"] = companion_ragged(lib, torch)
-        res["adjoint"] = companion_adjoint(lib, torch)
-        res["stream_conv"] = companion_stream_conv(lib, torch)
+        wanted = set(COMPANIONS) if args.companions == "all" else set(args.companions.split(","))
+        for name, fn in COMPANIONS.items():
+            if name in wanted:
+                res[name] = fn(lib, torch)
     return res
 
 
@@ -652,6 +650,16 @@ def companion_adjoint(lib, torch) -> dict:
             "fft_GFLOP/s": fft_flops / (ms * 1e-3) / 1e9}
 
 
+COMPANIONS = {
+    "batched_1024": companion_batched_1024,
+    "fft2d_4096": companion_2d,
+    "split_tc": companion_split,
+    "ragged_conv": companion_ragged,
+    "adjoint": companion_adjoint,
+    "stream_conv": companion_stream_conv,
+}
+
+
 def run_reference(args, world, rank, pg) -> dict | None:
     if rank != 0:
         return None
@@ -688,6 +696,8 @@ def main():
                     help="run the workload's plan in split precision on the tensor cores (N = 256 or 4096)")
     ap.add_argument("--no-companions", action="store_true",
                     help="skip the split-precision, ragged-convolution and adjoint measurements")
+    ap.add_argument("--companions", default="all",
+                    help="comma-separated companion measurements to run (default all: " + ",".join(COMPANIONS) + ")")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local, pg = dist_setup()

@@ -107,12 +107,15 @@ __global__ void upols_mac(float2 *__restrict__ y, const float2 *__restrict__ xcu
     if (b < nb) {
         const float2 x = xcur[b];
         float2 acc = make_float2(0.f, 0.f);
+        unsigned slot = (cur + P - p0 % P) % P;  // slot of block k - p0
+        // unrolled so that several partitions' loads are in flight at once
+#pragma unroll 4
         for (unsigned p = p0; p < p1; p++) {
-            const unsigned slot = (cur + P - p) % P;  // block k - p
-            const float2 xp = p == 0 ? x : fdl[(size_t)slot * nb + b];
-            const float2 hp = h[(size_t)p * nb + b];
+            const float2 xp = p == 0 ? x : __ldcg(&fdl[(size_t)slot * nb + b]);
+            const float2 hp = __ldg(&h[(size_t)p * nb + b]);
             acc.x += xp.x * hp.x - xp.y * hp.y;
             acc.y += xp.x * hp.y + xp.y * hp.x;
+            slot = slot ? slot - 1 : P - 1;  // block k - p - 1
         }
         part[(size_t)g * nb + b] = acc;
         if (g == 0)
