@@ -74,6 +74,10 @@ mufft_plan_1d *mufft_gb_create_plan_1d_c2r_batched(unsigned N, unsigned flags,
  * must not overlap on the GPU (enqueue them on one stream). */
 int mufft_gb_execute_plan_1d_async(mufft_plan_1d *plan, void *output, const void *input, void *stream);
 int mufft_gb_execute_plan_2d_async(mufft_plan_2d *plan, void *output, const void *input, void *stream);
+/* Enqueues only launches first .. first + count - 1 of a 2D plan (device
+ * buffers; for timing one pass at a time, like the 1D variant). */
+int mufft_gb_execute_plan_2d_launches_async(mufft_plan_2d *plan, void *output, const void *input, unsigned first,
+                                            unsigned count, void *stream);
 int mufft_gb_execute_conv_input_async(mufft_plan_conv *plan, unsigned block, void *output,
                                       const void *input, void *stream);
 int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, const void *input_first,
@@ -266,6 +270,10 @@ int mufft_gb_autotune_save(const char *path);
 int mufft_gb_autotune_load(const char *path);
 void mufft_gb_autotune_clear(void);
 
+/* Columns of 2D plans created afterwards: 0 automatic (columns of 8192 points
+ * and more as a two-pass four-step of short, wide column tiles), 1 one pass of
+ * whole-column tiles, 2 the two-pass form whenever the column length allows. */
+int mufft_gb_set_2d_columns(int mode);
 /* Column passes of multi-pass plans created afterwards stage each tile
  * through a TMA tensor copy into shared memory, double-buffered in
  * persistent CTAs (1) or single-buffered (2), or load it with per-thread

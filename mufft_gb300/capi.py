@@ -79,6 +79,7 @@ GB_H = [
     ("execute_conv_output_async", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("plan_1d_launches", _u, [_vp]),
     ("plan_2d_launches", _u, [_vp]),
+    ("execute_plan_2d_launches_async", _i, [_vp, _vp, _vp, _u, _u, _vp]),
     ("plan_1d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("plan_2d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, C.c_char_p, _sz]),
@@ -92,6 +93,7 @@ GB_H = [
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
     ("set_split_engine", _i, [_i]),
     ("set_tma", _i, [_i]),
+    ("set_2d_columns", _i, [_i]),
     ("autotune_1d", _i, [_i, _u, _i, _u, _u, _vp, _sz]),
     ("autotune_save", _i, [C.c_char_p]),
     ("autotune_load", _i, [C.c_char_p]),

@@ -301,7 +301,7 @@ bool is_device_accessible(const void *p)
 
 // ================================================================ passes
 
-enum Role { ROLE_NONE = 0, ROLE_IN, ROLE_OUT, ROLE_IN2, ROLE_SCRATCH };
+enum Role { ROLE_NONE = 0, ROLE_IN, ROLE_OUT, ROLE_IN2, ROLE_SCRATCH, ROLE_SCRATCH2 };
 enum PassType { PASS_TILE = 0, PASS_R2C_FIXUP = 1, PASS_BC = 2, PASS_SPLIT = 3 };
 
 struct Pass {
@@ -334,6 +334,7 @@ struct Buffers {
     void *out;
     const void *in2;
     void *scratch;
+    void *scratch2 = nullptr;
 };
 
 const void *pick(Role r, const Buffers &b)
@@ -343,6 +344,7 @@ const void *pick(Role r, const Buffers &b)
     case ROLE_OUT: return b.out;
     case ROLE_IN2: return b.in2;
     case ROLE_SCRATCH: return b.scratch;
+    case ROLE_SCRATCH2: return b.scratch2;
     default: return nullptr;
     }
 }
@@ -422,7 +424,7 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                 }
             }
             void *args[] = {&a};
-            const size_t smem = (a.tw_lo || a.tw_colpow) ? p.k->smem : p.k->smem_ex;
+            const size_t smem = (a.tw_lo || a.tw_colpow || a.tw_by_y) ? p.k->smem : p.k->smem_ex;
             cudaError_t e;
             if (p.k->Q > 1) {
                 // one tile per cluster of Q CTAs (distributed shared memory)
@@ -538,6 +540,7 @@ struct PlanResources {
     float2 *twlo2 = nullptr;  // three-level: the same for the second column pass
     float2 *scratch = nullptr;
     size_t scratch_bytes = 0;
+    float2 *scratch2 = nullptr;   // 2D plans whose columns run as a two-pass four-step
     float2 *ring = nullptr;       // fused B/C: L2-resident ring of row blocks
     unsigned *counters = nullptr; // fused B/C: task counters
     int *err = nullptr;           // device error flag of bounded waits
@@ -556,10 +559,11 @@ struct PlanResources {
         cudaFree(twlo);
         cudaFree(twlo2);
         cudaFree(scratch);
+        cudaFree(scratch2);
         cudaFree(ring);
         cudaFree(counters);
         cudaFree(err);
-        rtw = twlo = twlo2 = scratch = ring = nullptr;
+        rtw = twlo = twlo2 = scratch = scratch2 = ring = nullptr;
         counters = nullptr;
         err = nullptr;
     }
@@ -579,6 +583,9 @@ std::atomic<int> g_twiddle_table{-1};
 // default: the separate passes measured faster on GB300 -- they are bound by
 // instruction issue and latency, not by the HBM traffic the fusion saves).
 std::atomic<int> g_fused_bc{0};
+// 2D columns: 0 automatic (two-pass four-step from 8192 points), 1 one column
+// pass, 2 the two-pass form whenever possible (set with mufft_gb_set_2d_columns).
+std::atomic<int> g_2d_columns{0};
 // Split-precision products on tcgen05.mma (0, default) or warp-level mma.sync (1).
 std::atomic<int> g_split_engine{0};
 
@@ -2569,6 +2576,81 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         pl->out_width = pl->out_pitch = (size_t)Nx * 4;
     }
     col.grid = dim3((col.a.ntrans + kcol->C - 1) / kcol->C, 1);
+
+    // Long columns: a four-step along the columns, Ny = N1 x N2, in two
+    // passes of short column tiles (C1: length N1 at stride N2 rows, twiddle
+    // W_Ny^(k1*n2) with n2 the grid row; C2: length N2, stored transposed to
+    // rows k1 + N1*k2) -- 64-column tiles instead of the 1-2-column tiles a
+    // whole 8192- or 16384-point column allows.  At Ny = 4096 the one-pass
+    // 4-column tiles measured as fast or faster (4096^2 r2c columns 41.3 us
+    // vs 18.6 + 26.8 us; c2c 84.8 vs 53.4 + 43.2 us), so the automatic choice
+    // starts at 8192.
+    const int mode = g_2d_columns.load();
+    const unsigned lgy = ilog2u(Ny);
+    const unsigned N1 = 1u << (lgy / 2), N2 = Ny / N1;
+    const TileKernel *kc1 = find_tile((int)N1, ACROSS, ACROSS), *kc2 = find_tile((int)N2, ACROSS, ACROSS);
+    if ((mode == 2 || (mode == 0 && Ny >= 8192)) && N1 >= 2 && kc1 && kc2) {
+        const unsigned ncols = (unsigned)col.a.ntrans;
+        const long long s_in = col.a.in_stride;                                 // pitch the columns are read at
+        const long long s_out = kind == K2_C2R ? (long long)(Mx + 1) : (long long)Nx;  // pitch of C1 / C2 outputs
+        const Role c1_in = kind == K2_C2R ? ROLE_IN : ROLE_SCRATCH;
+        const Role c1_out = ROLE_SCRATCH;
+        const Role c2_out = kind == K2_C2R ? ROLE_SCRATCH2 : ROLE_OUT;
+        const size_t bytes = (size_t)Ny * (size_t)s_out * sizeof(float2);
+        if (kind != K2_C2R) {
+            cudaFree(pl->res.scratch);
+            pl->res.scratch = nullptr;
+        }
+        if ((!pl->res.scratch && !cuda_ok(cudaMalloc(&pl->res.scratch, bytes), "cudaMalloc(scratch)")) ||
+            (kind == K2_C2R && !cuda_ok(cudaMalloc(&pl->res.scratch2, bytes), "cudaMalloc(scratch)"))) {
+            destroy_2d(pl);
+            return nullptr;
+        }
+        Pass c1;
+        c1.k = kc1;
+        c1.a.tw = tw;
+        c1.a.scale = 1.0f;
+        c1.a.in_stride = (long long)N2 * s_in;
+        c1.a.out_stride = (long long)N2 * s_out;
+        c1.a.in_dist = c1.a.out_dist = 1;
+        c1.a.in_batch = s_in;
+        c1.a.out_batch = s_out;
+        c1.a.ntrans = ncols;
+        c1.a.conj = (col.a.conj & 1);
+        c1.a.epilogue = EPI_TWIDDLE;
+        c1.a.tw_by_y = 1;
+        c1.a.tw_scale = 2.0f / (float)Ny;
+        c1.a.tw_mask = Ny - 1;
+        c1.in_role = c1_in;
+        c1.out_role = c1_out;
+        c1.grid = dim3((ncols + kc1->C - 1) / kc1->C, N2);
+        Pass c2;
+        c2.k = kc2;
+        c2.a.tw = tw;
+        c2.a.scale = 1.0f;
+        c2.a.in_stride = s_out;
+        c2.a.out_stride = (long long)N1 * s_out;
+        c2.a.in_dist = c2.a.out_dist = 1;
+        c2.a.in_batch = (long long)N2 * s_out;
+        c2.a.out_batch = s_out;
+        c2.a.ntrans = ncols;
+        c2.a.conj = (col.a.conj & 2);
+        c2.in_role = ROLE_SCRATCH;
+        c2.out_role = c2_out;
+        c2.grid = dim3((ncols + kc2->C - 1) / kc2->C, N1);
+        if (kind == K2_C2R) {
+            row.in_role = ROLE_SCRATCH2;
+            pl->passes.push_back(c1);
+            pl->passes.push_back(c2);
+            pl->passes.push_back(row);
+        } else {
+            row.out_role = ROLE_SCRATCH;
+            pl->passes.push_back(row);
+            pl->passes.push_back(c1);
+            pl->passes.push_back(c2);
+        }
+        return pl;
+    }
     if (kind == K2_C2R) {
         pl->passes.push_back(col);
         pl->passes.push_back(row);
@@ -2594,7 +2676,7 @@ int exec_2d(mufft_plan_2d *pl, void *out, const void *in, cudaStream_t st, bool 
     }
     if (sync)
         st = pl->stream;
-    Buffers b{in, out, nullptr, pl->res.scratch};
+    Buffers b{in, out, nullptr, pl->res.scratch, pl->res.scratch2};
     const size_t in_bytes = pl->in_rows * pl->in_pitch;
     const size_t out_bytes = pl->out_rows * pl->out_pitch;
     if (hin) {
@@ -2649,6 +2731,20 @@ void mufft_execute_plan_2d(mufft_plan_2d *plan, void *MUFFT_RESTRICT output, con
 int mufft_gb_execute_plan_2d_async(mufft_plan_2d *plan, void *output, const void *input, void *stream)
 {
     return exec_2d(plan, output, input, (cudaStream_t)stream, false);
+}
+
+int mufft_gb_execute_plan_2d_launches_async(mufft_plan_2d *plan, void *output, const void *input, unsigned first,
+                                            unsigned count, void *stream)
+{
+    if (!plan || !is_device_accessible(output) || !is_device_accessible(input)) {
+        set_error(MUFFT_GB_ERR_INVALID, "needs a plan and device buffers");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(plan->device);
+    Buffers b{input, output, nullptr, plan->res.scratch, plan->res.scratch2};
+    if (!cuda_ok(run_passes(plan->passes, b, (cudaStream_t)stream, first, count), "kernel launch"))
+        return t_err;
+    return MUFFT_GB_OK;
 }
 
 void mufft_free_plan_2d(mufft_plan_2d *plan) { destroy_2d(plan); }
@@ -2892,6 +2988,16 @@ int mufft_gb_set_conv_split(unsigned points)
         return MUFFT_GB_ERR_INVALID;
     }
     g_conv_split_lg.store(points ? ilog2u(points) : 17u);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_2d_columns(int mode)
+{
+    if (mode < 0 || mode > 2) {
+        set_error(MUFFT_GB_ERR_INVALID, "mode must be 0 (automatic), 1 (one pass) or 2 (two passes)");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_2d_columns.store(mode);
     return MUFFT_GB_OK;
 }
 

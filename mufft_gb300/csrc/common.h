@@ -87,6 +87,10 @@ struct TileArgs {
     // nonzero: per-tile column powers instead (W_N^(col*off) for the R output
     // offsets of each column in shared memory, times W_N^(col*base) per thread)
     int tw_colpow;
+    // nonzero: the twiddle's column factor is the CTA's grid row instead of the
+    // transform index (column passes of a 2D four-step: W_N^(k*row) for every
+    // column of the tile, from a per-CTA table)
+    int tw_by_y;
 };
 
 }  // namespace mgb

@@ -563,7 +563,7 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // L2-coherent loads (input written earlier in the same launch).
 template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
-                                          float2 *smem, const float2 *sin = nullptr)
+                                          float2 *smem, const float2 *sin = nullptr, unsigned twy = 0)
 {
     using S = Sched<L, R>;
     using TT = Tile<L, R, Q>;
@@ -580,7 +580,13 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     static_assert(tile_smem_bytes<L, R, C, Q, LMAP, SMAP>() <= kMaxSmemPerCta, "tile exceeds shared memory");
     if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
         float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
-        if (a.epilogue == EPI_TWIDDLE && a.tw_colpow) {
+        if (a.epilogue == EPI_TWIDDLE && a.tw_by_y) {
+            // W_N^(k*row) for every output k, the same for all columns
+            for (int k = threadIdx.x; k < L; k += tile_threads<L, R, C, Q>())
+                thi[k] = fourstep_twiddle((unsigned)k * twy, a.tw_scale, a.tw_mask);
+            if constexpr (NST == 1)
+                __syncthreads();
+        } else if (a.epilogue == EPI_TWIDDLE && a.tw_colpow) {
             // W_N^(col*off_i), col = tile*C + c, for the last stage's output
             // offsets off_i = TL*u + m*BL of register i = u*rl + m
             constexpr int rl = S::radix(NST - 1), BL = TT::B(NST - 1);
@@ -694,7 +700,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
             float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
             float2 wbase = make_float2(1.f, 0.f);
             if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
-                if (a.tw_colpow)
+                if (a.tw_colpow && !a.tw_by_y)
                     wbase = fourstep_twiddle((unsigned)p0 * tr, a.tw_scale, a.tw_mask);
             }
 #pragma unroll
@@ -705,14 +711,16 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     const int k = p0 + off;
                     float2 w;
                     if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
-                        if (a.tw_colpow)
+                        if (a.tw_by_y)
+                            w = thi[k];
+                        else if (a.tw_colpow)
                             w = cmul(wbase, thi[(u * rl + m) * C + c]);
                         else if (a.tw_lo)
                             w = cmul(__ldg(&a.tw_lo[k * C + c]), thi[k]);
                         else
                             w = fourstep_twiddle((unsigned)k * tr, a.tw_scale, a.tw_mask);
                     } else {
-                        w = fourstep_twiddle((unsigned)k * tr, a.tw_scale, a.tw_mask);
+                        w = fourstep_twiddle((unsigned)k * (a.tw_by_y ? twy : tr), a.tw_scale, a.tw_mask);
                     }
                     float2 y = cmul(v[u * rl + m], w);
                     if (a.conj & 2)
@@ -754,7 +762,7 @@ __global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L,
         j = (int)cg::this_cluster().block_rank();
         tile = blockIdx.x / Q;
     }
-    tile_body<L, R, C, Q, LMAP, SMAP, false>(a, tile, j, ioff, ooff, smem);
+    tile_body<L, R, C, Q, LMAP, SMAP, false>(a, tile, j, ioff, ooff, smem, nullptr, blockIdx.y);
 }
 
 }  // namespace mgb

@@ -95,3 +95,25 @@ def test_large_batches_of_tiny_transforms(gpu, torch, N, B):
     rows = np.r_[0:4, B // 2:B // 2 + 4, B - 4:B]
     ref = np.fft.ifft(x[rows].astype(np.complex128), axis=1) * N
     assert rel_l2(y[rows], ref) < 2e-6
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("Nx,Ny", [(64, 64), (16, 2048), (4096, 4096), (2048, 8192), (8, 16384)])
+def test_2d_column_schedules(gpu, mode, Nx, Ny):
+    """2D columns as one pass of whole-column tiles (1) or as the two-pass
+    four-step along the columns (2): c2c both directions, r2c and c2r."""
+    try:
+        assert gpu.gb_set_2d_columns(mode) == 0
+        x = signals.complex_uniform(75000 + Nx + Ny, Nx * Ny).reshape(Ny, Nx)
+        ref = np.fft.fft2(x.astype(np.complex128))
+        got = gpu.fft2_c2c(x, K.FORWARD)
+        assert rel_l2(got, ref) < 2e-6
+        inv = gpu.fft2_c2c(got, K.INVERSE)
+        assert rel_l2(inv / (Nx * Ny), x) < 4e-6
+        xr = signals.uniform(75100 + Nx + Ny, Nx * Ny).reshape(Ny, Nx)
+        X = gpu.fft2_r2c(xr)
+        assert rel_l2(X[:, : Nx // 2 + 1], np.fft.rfft2(xr.astype(np.float64))) < 2e-6
+        back = gpu.fft2_c2r(X)
+        assert rel_l2(back / (Nx * Ny), xr) < 4e-6
+    finally:
+        gpu.gb_set_2d_columns(0)
