@@ -450,6 +450,8 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
             SplitArgs a = p.sp;
             a.in = (const float2 *)pick(p.in_role, b);
             a.out = (float2 *)pick(p.out_role, b);
+            // bulk async copies need 16-byte aligned transforms
+            a.bulk = (((uintptr_t)a.in & 15) == 0 && (a.in_dist & 1) == 0) ? 1 : 0;
             void *args[] = {&a};
             cudaError_t e =
                 p.sp_engine == 0

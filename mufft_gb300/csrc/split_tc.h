@@ -18,6 +18,7 @@ struct SplitArgs {
     const float2 *tw;             // stage twiddle factors: W_256^(m*q) then W_4096^(m*r), m, q, r < 16
     const void *bfrag;            // tcgen05 form: DFT-16 limbs as B operands (core-matrix order)
     int *err;                     // tcgen05 form: set when a bounded wait times out
+    int bulk;                     // tcgen05 form: inputs 16-byte aligned, prefetched by bulk async copies
 };
 
 constexpr int kSplitThreads = 256;

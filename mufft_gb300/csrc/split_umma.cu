@@ -42,7 +42,7 @@ constexpr int kBOff = kAOff + 3 * 2 * kATile;      // [limb] B operands: 3 x 2 K
 constexpr int kXOff = kBOff + 3 * 2048;            // exchange: 4096 points padded
 constexpr int kXElems = 4096 + 256;                // upad(4095) + 1
 constexpr int kTwOff = kXOff + kXElems * 8;        // 512 stage twiddle factors
-constexpr int kBarOff = kTwOff + 512 * 8;          // mbarrier (8 B) + TMEM address (4 B)
+constexpr int kBarOff = kTwOff + 512 * 8;          // 3 mbarriers (24 B) + TMEM address (4 B)
 constexpr int kUSmem = kBarOff + 64;
 
 __device__ __forceinline__ int upad(int e) { return e + (e >> 4); }
@@ -153,6 +153,29 @@ __device__ __forceinline__ void split2(float a, float b, unsigned (&o)[LIMBS])
     }
 }
 
+// Bulk copy of `bytes` contiguous bytes into shared memory, completing on `bar`.
+__device__ __forceinline__ void bulk_copy(unsigned dst, const void *src, unsigned bytes, unsigned bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// Issues the copies of block `blk`'s transforms into the staging area (thread 0).
+template <int N, int T>
+__device__ __forceinline__ void prefetch_block(const SplitArgs &a, long long blk, unsigned stage, unsigned bar)
+{
+    const long long tr0 = blk * T;
+    const unsigned nt = (unsigned)((a.ntrans - tr0) < T ? (a.ntrans - tr0) : T);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(nt * (unsigned)(N * sizeof(float2)))
+                 : "memory");
+    for (unsigned t = 0; t < nt; t++)
+        bulk_copy(stage + t * (unsigned)(N * sizeof(float2)), a.in + (tr0 + t) * a.in_dist,
+                  (unsigned)(N * sizeof(float2)), bar);
+}
+
 template <int S, int LIMBS>
 __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a)
 {
@@ -166,9 +189,14 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
     extern __shared__ __align__(1024) unsigned char sm[];
     float2 *X = (float2 *)(sm + kXOff);
     float2 *t1 = (float2 *)(sm + kTwOff), *t2 = t1 + 256;
-    const unsigned bar = smem_u32(sm + kBarOff);
-    unsigned *tmem_slot = (unsigned *)(sm + kBarOff + 8);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    // mbarriers: [0], [1] MMA completion of tiles 0 and 1, [2] input prefetch
+    const unsigned bar0 = smem_u32(sm + kBarOff), bar_in = bar0 + 16;
+    unsigned *tmem_slot = (unsigned *)(sm + kBarOff + 24);
+    // the next block's input lands in the A-operand region once the last
+    // stage's products are done with it
+    const float2 *stage_in = (const float2 *)(sm + kAOff);
+    const int tid = threadIdx.x, warp = tid >> 5, half = tid >> 7;
+    const bool bulk = a.bulk != 0;
 
     // B operands (F limbs, already in core-matrix order) and stage twiddles
     for (int i = tid; i < 3 * 2048 / 16; i += kUThreads)
@@ -176,7 +204,8 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
     for (int i = tid; i < 512; i += kUThreads)
         t1[i] = __ldg(&a.tw[i]);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1));
+        for (int b = 0; b < 3; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar0 + 8 * b), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -188,20 +217,43 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
     __syncthreads();
     fence_after();
     const unsigned tmem = *tmem_slot;
-    unsigned phase = 0;
-    bool ok = true;
+    unsigned phase = 0, in_phase = 0;
+    bool ok = true, in_flight = false;
 
     const long long nblocks = ((long long)a.ntrans + T - 1) / T;
+    if (bulk && tid == 0 && (long long)blockIdx.x < nblocks) {
+        prefetch_block<N, T>(a, blockIdx.x, smem_u32(stage_in), bar_in);
+        in_flight = true;
+    }
+    in_flight = __syncthreads_or(in_flight) != 0;
     for (long long blk = blockIdx.x; blk < nblocks && ok; blk += gridDim.x) {
         const long long tr0 = blk * T;
-        for (int e = tid; e < 4096; e += kUThreads) {
-            const int t = e / N, n = e % N;
-            float2 v = make_float2(0.f, 0.f);
-            if (tr0 + t < a.ntrans)
-                v = __ldg(&a.in[(tr0 + t) * a.in_dist + n]);
-            if (a.conj)
-                v.y = -v.y;
-            X[upad(e)] = v;
+        if (bulk) {
+            ok = __syncthreads_and(tid == 0 ? bar_wait(bar_in, in_phase & 1) : true) != 0;
+            if (!ok) {
+                if (tid == 0 && a.err)
+                    atomicExch(a.err, 1);
+                break;
+            }
+            in_phase++;
+            in_flight = false;
+            for (int e = tid; e < 4096; e += kUThreads) {
+                const int t = e / N;
+                float2 v = tr0 + t < a.ntrans ? stage_in[e] : make_float2(0.f, 0.f);
+                if (a.conj)
+                    v.y = -v.y;
+                X[upad(e)] = v;
+            }
+        } else {
+            for (int e = tid; e < 4096; e += kUThreads) {
+                const int t = e / N, n = e % N;
+                float2 v = make_float2(0.f, 0.f);
+                if (tr0 + t < a.ntrans)
+                    v = __ldg(&a.in[(tr0 + t) * a.in_dist + n]);
+                if (a.conj)
+                    v.y = -v.y;
+                X[upad(e)] = v;
+            }
         }
         __syncthreads();
 
@@ -241,24 +293,24 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             fence_before();
-            __syncthreads();
-            if (tid == 0) {
+            // each half of the CTA owns one M = 128 tile: its products start as
+            // soon as that half has written its operands
+            asm volatile("bar.sync %0, 128;" ::"r"(1 + half) : "memory");
+            if ((tid & 127) == 0) {
                 fence_after();
 #pragma unroll
-                for (int tl = 0; tl < 2; tl++)
+                for (int q = 0; q < NT; q++)
 #pragma unroll
-                    for (int q = 0; q < NT; q++)
-#pragma unroll
-                        for (int kh = 0; kh < 2; kh++) {
-                            const unsigned aaddr = smem_u32(sm + kAOff + tb[q] * 2 * kATile + tl * kATile + kh * 256);
-                            const unsigned baddr = smem_u32(sm + kBOff + ta[q] * 2048 + kh * 256);
-                            umma(tmem + tl * 32, umma_desc(aaddr), umma_desc(baddr), (q | kh) ? 1u : 0u);
-                        }
-                umma_commit(bar);
+                    for (int kh = 0; kh < 2; kh++) {
+                        const unsigned aaddr = smem_u32(sm + kAOff + tb[q] * 2 * kATile + half * kATile + kh * 256);
+                        const unsigned baddr = smem_u32(sm + kBOff + ta[q] * 2048 + kh * 256);
+                        umma(tmem + half * 32, umma_desc(aaddr), umma_desc(baddr), (q | kh) ? 1u : 0u);
+                    }
+                umma_commit(bar0 + 8 * half);
             }
-            // one thread waits for the commit (the others block in the barrier
-            // without issuing); the outcome is made CTA-uniform
-            ok = __syncthreads_and(tid == 0 ? bar_wait(bar, phase & 1) : true) != 0;
+            // every gather of this stage is done before any scatter below; one
+            // thread per half waits for its tile's commit
+            ok = __syncthreads_and((tid & 127) == 0 ? bar_wait(bar0 + 8 * half, phase & 1) : true) != 0;
             if (!ok) {
                 if (tid == 0 && a.err)
                     atomicExch(a.err, 1);
@@ -267,10 +319,14 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
             }
             fence_after();
             if (ok) {
+                if (s == S - 1 && bulk && tid == 0 && blk + gridDim.x < nblocks) {
+                    // every product of this block is done: the A region is free
+                    prefetch_block<N, T>(a, blk + gridDim.x, smem_u32(stage_in), bar_in);
+                    in_flight = true;
+                }
                 // D row of this thread's column: lane group (warp & 3), tile (warp >> 2)
                 float d[32];
                 tmem_ld32(tmem + ((unsigned)((warp & 3) * 32) << 16) + (warp >> 2) * 32, d);
-                // every read of X for this stage is complete (barrier above): scatter
 #pragma unroll
                 for (int k = 0; k < 16; k++) {
                     const int pos = tt * N + (j / p) * 16 * p + (j & (p - 1)) + k * p;
@@ -291,12 +347,18 @@ __global__ void __launch_bounds__(kUThreads, 2) split_umma_fft(const SplitArgs a
                 }
             }
         }
-        __syncthreads();
+        in_flight = __syncthreads_or(in_flight) != 0;
     }
     if (!ok) {
-        // let this CTA's MMAs drain before TMEM is released (bounded): the
-        // timed-out phase is still `phase`
-        bar_wait(bar, phase & 1);
+        // let this CTA's products and copies drain before TMEM is released
+        // (bounded): the timed-out phases are still `phase` / `in_phase`
+        if (tid == 0) {
+            bar_wait(bar0, phase & 1);
+            bar_wait(bar0 + 8, phase & 1);
+            if (in_flight)
+                bar_wait(bar_in, in_phase & 1);
+        }
+        __syncthreads();
     }
     fence_before();
     __syncthreads();

@@ -85,9 +85,11 @@ def test_split_bf16x2_error(gpu, torch, engine, N, B, kind):
         assert 1e-7 < e < 5e-5, e  # two limbs: ~16 significant bits
 
 
-def test_split_strided_batch(gpu, torch, engine):
-    """Padded batch distances go through the split path too."""
-    N, B, dist = 4096, 5, 4096 + 64
+@pytest.mark.parametrize("N,dist", [(4096, 4096 + 64), (4096, 4097), (256, 257), (256, 300)])
+def test_split_strided_batch(gpu, torch, engine, N, dist):
+    """Padded batch distances go through the split path too (odd distances
+    take the per-thread loads instead of bulk copies)."""
+    B = 5
     x = np.zeros((B, dist), np.complex64)
     x[:, :N] = signals.complex_uniform(42000, B * N).reshape(B, N)
     dx = torch.from_numpy(x).cuda()
