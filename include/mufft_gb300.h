@@ -145,18 +145,27 @@ typedef struct mufft_gb_conv_request {
 typedef struct mufft_gb_conv_batch mufft_gb_conv_batch;
 
 /* Prepares `count` requests of mixed sizes for one persistent launch,
- * captured in a CUDA graph.  Requests are ordered longest first; those of at
- * least the split size (2^16 complex points by default) run as phase tasks
- * spread over many CTAs, the others whole in one CTA each.  flags: 0, or
- * MUFFT_GB_FLAG_AUTOTUNE to time the batch with every split size (running
- * it, so writing the outputs, a few times) and keep the fastest. */
+ * captured in a CUDA graph.  Requests of 16384 complex points and more run
+ * as class pipelines (mufft_gb_set_conv_classes); the rest, longest first,
+ * in a persistent kernel, whole in one CTA each or -- from the split size --
+ * as phase tasks spread over many CTAs.  flags: 0, or MUFFT_GB_FLAG_AUTOTUNE
+ * to time the batch with every split / class size (running it, so writing
+ * the outputs, a few times) and keep the fastest. */
 mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *requests, unsigned count,
                                                 unsigned flags);
 /* Default split size of batches created afterwards: a power of two in
  * 16384..65536 complex points, or 0 to run every request whole. */
 int mufft_gb_set_conv_split(unsigned points);
+/* Requests of at least this many complex points (16384..65536, default
+ * 16384; 0: none) in batches created afterwards run as class pipelines: the requests
+ * of one size, method and zero-pad setting go through five ordinary batched
+ * launches (the four-step phases), on parallel branches of the batch's graph,
+ * beside the persistent kernel that runs the rest. */
+int mufft_gb_set_conv_classes(unsigned points);
 /* The split size in use (complex points; 0: no request is split). */
 unsigned mufft_gb_conv_batch_split_size(const mufft_gb_conv_batch *batch);
+/* The class-pipeline size in use (complex points; 0: none). */
+unsigned mufft_gb_conv_batch_class_size(const mufft_gb_conv_batch *batch);
 /* Synchronises the device and reports whether a bounded wait of the batch's
  * task dependencies timed out in an earlier execute (MUFFT_GB_ERR_UNSUPPORTED),
  * clearing the flag. */

@@ -107,8 +107,10 @@ GB_H = [
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),
     ("conv_batch_split_size", _u, [_vp]),
+    ("conv_batch_class_size", _u, [_vp]),
     ("conv_batch_status", _i, [_vp]),
     ("set_conv_split", _i, [_u]),
+    ("set_conv_classes", _i, [_u]),
     ("free_conv_batch", None, [_vp]),
     ("device_alloc", _vp, [_sz]),
     ("device_free", None, [_vp]),

@@ -1943,9 +1943,16 @@ struct mufft_gb_conv_batch {
     cudaGraphExec_t exec = nullptr;
     unsigned grid = 0;
     unsigned split_lg = 16;          // requests of 2^split_lg complex points and more run as phase tasks
+    unsigned class_lg = 14;          // requests of 2^class_lg points and more run as class pipelines
+    unsigned small_grid = 0;         // persistent CTAs when class pipelines run beside them (0: all SMs)
     std::vector<RaggedReq> sorted;   // longest first (host copy)
     RaggedArgs args{};
     size_t smem = 0;
+    ClassEntry *d_class = nullptr;
+    std::vector<cudaStream_t> class_streams;
+    std::vector<cudaEvent_t> class_events;
+    cudaEvent_t fork_event = nullptr;
+    int sms = 0;
 };
 
 namespace {
@@ -1962,6 +1969,13 @@ void destroy_conv_batch(mufft_gb_conv_batch *b)
             cudaGraphDestroy(b->graph);
         if (b->capture)
             cudaStreamDestroy(b->capture);
+        for (cudaStream_t cs : b->class_streams)
+            cudaStreamDestroy(cs);
+        for (cudaEvent_t ev : b->class_events)
+            cudaEventDestroy(ev);
+        if (b->fork_event)
+            cudaEventDestroy(b->fork_event);
+        cudaFree(b->d_class);
         cudaFree(b->d_reqs);
         cudaFree(b->d_tasks);
         cudaFree(b->d_err);
@@ -1978,10 +1992,63 @@ void destroy_conv_batch(mufft_gb_conv_batch *b)
 // requests took the batch from 0.19 to 0.177 ms, splitting 32768 and 16384
 // as well cost more in task overhead than it gained (0.226, 0.259 ms).
 std::atomic<unsigned> g_conv_split_lg{16};
+// Requests of 2^g_conv_class_lg complex points and more run as class
+// pipelines (ordinary batched launches per size class; 17: none).  Default
+// 2^14: on the 512-request mix the batch went from 0.177 ms (split tasks for
+// 65536) to 0.152 / 0.148 / 0.146 ms with classes from 65536 / 32768 / 16384.
+std::atomic<unsigned> g_conv_class_lg{14};
 
 // Task list for a split size, uploaded with the request table, and the graph
 // (counter resets + the persistent launch) that replays it.
-bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg)
+// Launches of one class pipeline (five four-step phases over the class's
+// requests) on `st`.
+bool enqueue_class(mufft_gb_conv_batch *b, unsigned lg, bool stereo, bool zp, const ClassEntry *tab, unsigned K,
+                   cudaStream_t st)
+{
+    const int L1 = lg == 16 ? 256 : 128, L2 = lg == 14 ? 128 : 256, L = L1 * L2;
+    const ClassTile ct = class_column_tile(L1), rt = class_row_tile(L2);
+    TileArgs base{};
+    base.tw = g_dev[b->device].tw;
+    base.scale = 1.0f;
+    base.tw_scale = 2.0f / (float)L;
+    base.tw_mask = (unsigned)(L - 1);
+    TileArgs cols = base, rows = base;
+    cols.in_stride = cols.out_stride = L2;
+    cols.in_dist = cols.out_dist = 1;
+    cols.ntrans = (unsigned)L2;
+    rows.in_stride = rows.out_stride = 1;
+    rows.in_dist = rows.out_dist = L2;
+    rows.ntrans = (unsigned)L1;
+    TileArgs ph[5] = {cols, rows, base, rows, cols};
+    ph[0].half = zp ? 1 : 0;
+    ph[0].epilogue = EPI_TWIDDLE;
+    ph[0].tw_colpow = 1;
+    ph[3].conj = 1;
+    ph[3].epilogue = EPI_TWIDDLE;
+    ph[4].conj = 2;
+    for (int phase = 0; phase < 5; phase++) {
+        cudaError_t e;
+        if (phase == 2) {
+            const unsigned l1 = ilog2u((unsigned)L1), l2 = ilog2u((unsigned)L2);
+            int st_ = stereo ? 1 : 0;
+            float scale = 1.0f / (float)(stereo ? L : 2 * L);
+            const float2 *rf = b->d_rtw + b->args.rtw_off[lg], *ri = rf + L;
+            void *args[] = {(void *)&tab, (void *)&l1, (void *)&l2, &st_, &scale, (void *)&rf, (void *)&ri};
+            e = cudaLaunchKernel(class_multiply_fn(), dim3((unsigned)(L / 2048), K), dim3(256), args, 0, st);
+        } else {
+            const ClassTile &t = (phase == 0 || phase == 4) ? ct : rt;
+            const unsigned tiles = (phase == 0 || phase == 4) ? (unsigned)(L2 / t.C) : (unsigned)(L1 / t.C);
+            int phase_ = phase;
+            void *args[] = {&ph[phase], (void *)&tab, &phase_};
+            e = cudaLaunchKernel(t.fn, dim3(tiles, K), dim3(t.threads), args, t.smem, st);
+        }
+        if (!cuda_ok(e, "class launch"))
+            return false;
+    }
+    return true;
+}
+
+bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_lg, unsigned small_grid)
 {
     DeviceGuard g(b->device);
     if (b->exec) {
@@ -1997,10 +2064,20 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg)
     b->d_tasks = nullptr;
     b->d_next = nullptr;
     b->split_lg = split_lg;
+    b->class_lg = class_lg;
+    b->small_grid = small_grid;
+    cudaFree(b->d_class);
+    b->d_class = nullptr;
     std::vector<RaggedReq> reqs = b->sorted;
     std::vector<unsigned> split_ids, whole_ids;
+    // class pipelines: (lg, stereo, zero pad) -> requests
+    std::map<std::tuple<unsigned, unsigned, unsigned>, std::vector<unsigned>> classes;
     unsigned nsplit = 0;
     for (unsigned i = 0; i < reqs.size(); i++) {
+        if (reqs[i].lg >= class_lg && reqs[i].lg >= kRaggedMinSplitLg) {
+            classes[std::make_tuple(reqs[i].lg, reqs[i].stereo, reqs[i].zero_pad)].push_back(i);
+            continue;
+        }
         reqs[i].split = reqs[i].lg >= split_lg && reqs[i].lg >= kRaggedMinSplitLg ? 1 : 0;
         if (reqs[i].split) {
             reqs[i].counter = 1 + nsplit++;
@@ -2025,7 +2102,31 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg)
             tasks.push_back(RaggedTask{whole_ids[w], 0, 0, 0, 0});
     }
     b->args.count = (unsigned)tasks.size();
-    if (!cuda_ok(cudaMalloc(&b->d_tasks, tasks.size() * sizeof(RaggedTask)), "cudaMalloc(tasks)") ||
+    std::vector<ClassEntry> entries;
+    std::vector<std::tuple<unsigned, unsigned, unsigned, size_t, unsigned>> class_list;  // lg, stereo, zp, offset, K
+    for (const auto &kv : classes) {
+        class_list.push_back(std::make_tuple(std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
+                                             entries.size(), (unsigned)kv.second.size()));
+        for (unsigned r : kv.second)
+            entries.push_back(ClassEntry{reqs[r].in, reqs[r].h, reqs[r].out, reqs[r].spec});
+    }
+    while (b->class_streams.size() < class_list.size()) {
+        cudaStream_t cs;
+        cudaEvent_t ev;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate") ||
+            !cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"))
+            return false;
+        b->class_streams.push_back(cs);
+        b->class_events.push_back(ev);
+    }
+    if (!b->fork_event && !cuda_ok(cudaEventCreateWithFlags(&b->fork_event, cudaEventDisableTiming), "cudaEventCreate"))
+        return false;
+    if (!entries.empty() &&
+        (!cuda_ok(cudaMalloc(&b->d_class, entries.size() * sizeof(ClassEntry)), "cudaMalloc(classes)") ||
+         !cuda_ok(cudaMemcpy(b->d_class, entries.data(), entries.size() * sizeof(ClassEntry), cudaMemcpyHostToDevice),
+                  "cudaMemcpy(classes)")))
+        return false;
+    if (!cuda_ok(cudaMalloc(&b->d_tasks, std::max<size_t>(1, tasks.size()) * sizeof(RaggedTask)), "cudaMalloc(tasks)") ||
         !cuda_ok(cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(RaggedTask), cudaMemcpyHostToDevice),
                  "cudaMemcpy(tasks)") ||
         !cuda_ok(cudaMemcpy(b->d_reqs, reqs.data(), reqs.size() * sizeof(RaggedReq), cudaMemcpyHostToDevice),
@@ -2036,13 +2137,28 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg)
     b->args.next = b->d_next;
     b->args.counters = b->d_next;
     b->args.err = b->d_err;
-    const unsigned grid = std::min<unsigned>(b->grid, (unsigned)tasks.size());
+    unsigned grid = std::min<unsigned>(b->grid, (unsigned)tasks.size());
+    if (!class_list.empty() && small_grid)
+        grid = std::min(grid, small_grid);
     void *kargs[] = {&b->args};
     bool ok = cuda_ok(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "capture") &&
-              cuda_ok(cudaMemsetAsync(b->d_next, 0, (1 + nsplit) * sizeof(unsigned), b->capture), "cudaMemsetAsync") &&
-              cuda_ok(cudaLaunchKernel(conv_ragged_fn(), dim3(grid), dim3(conv_ragged_threads()), kargs, b->smem,
-                                       b->capture),
-                      "kernel launch");
+              cuda_ok(cudaMemsetAsync(b->d_next, 0, (1 + nsplit) * sizeof(unsigned), b->capture), "cudaMemsetAsync");
+    // class pipelines on parallel branches, then the persistent kernel for the rest
+    if (ok && !class_list.empty())
+        ok = cuda_ok(cudaEventRecord(b->fork_event, b->capture), "fork");
+    for (size_t c = 0; ok && c < class_list.size(); c++) {
+        const auto &cl = class_list[c];
+        ok = cuda_ok(cudaStreamWaitEvent(b->class_streams[c], b->fork_event, 0), "fork") &&
+             enqueue_class(b, std::get<0>(cl), std::get<1>(cl) != 0, std::get<2>(cl) != 0, b->d_class + std::get<3>(cl),
+                           std::get<4>(cl), b->class_streams[c]) &&
+             cuda_ok(cudaEventRecord(b->class_events[c], b->class_streams[c]), "join");
+    }
+    if (ok && !tasks.empty())
+        ok = cuda_ok(cudaLaunchKernel(conv_ragged_fn(), dim3(grid), dim3(conv_ragged_threads()), kargs, b->smem,
+                                      b->capture),
+                     "kernel launch");
+    for (size_t c = 0; ok && c < class_list.size(); c++)
+        ok = cuda_ok(cudaStreamWaitEvent(b->capture, b->class_events[c], 0), "join");
     cudaGraph_t gr = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(b->capture, &gr);
     if (!ok || !cuda_ok(ce, "capture") || !cuda_ok(cudaGraphInstantiate(&b->exec, gr, 0), "cudaGraphInstantiate")) {
@@ -2148,17 +2264,30 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
         return nullptr;
     }
     b->grid = (unsigned)(sms * std::max(per_sm, 1));
+    b->sms = sms;
     b->args.reqs = b->d_reqs;
     b->args.tw = g_dev[dev].tw;
     b->args.rtw = b->d_rtw;
-    unsigned best_lg = g_conv_split_lg.load();
+    unsigned best_lg = g_conv_split_lg.load(), best_class = g_conv_class_lg.load(), best_small = 0;
     if (flags & MUFFT_GB_FLAG_AUTOTUNE) {
         // time the batch with every split size (17: nothing split) and keep the fastest
         cudaEvent_t e0, e1;
         double best = INFINITY;
         bool ok = cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") && cuda_ok(cudaEventCreate(&e1), "cudaEventCreate");
-        for (unsigned lg = kRaggedMinSplitLg; ok && lg <= 17; lg++) {
-            if (!conv_batch_build(b, lg)) {
+        struct Cand {
+            unsigned split_lg, class_lg, small_grid;
+        };
+        std::vector<Cand> cands;
+        for (unsigned lg = kRaggedMinSplitLg; lg <= 17; lg++)
+            cands.push_back(Cand{lg, 17, 0});
+        for (unsigned cl = kRaggedMinSplitLg; cl <= 16; cl++)
+            for (unsigned div : {1u, 2u, 4u})
+                cands.push_back(Cand{17, cl, (unsigned)b->sms / div});
+        Cand best_c{best_lg, g_conv_class_lg.load(), 0};
+        for (const Cand &cd : cands) {
+            if (!ok)
+                break;
+            if (!conv_batch_build(b, cd.split_lg, cd.class_lg, cd.small_grid)) {
                 ok = false;
                 break;
             }
@@ -2172,9 +2301,12 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
             ok = cuda_ok(cudaEventSynchronize(e1), "autotune") && cuda_ok(cudaEventElapsedTime(&ms, e0, e1), "autotune");
             if (ok && ms < best) {
                 best = ms;
-                best_lg = lg;
+                best_c = cd;
             }
         }
+        best_lg = best_c.split_lg;
+        best_class = best_c.class_lg;
+        best_small = best_c.small_grid;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (!ok) {
@@ -2182,7 +2314,7 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
             return nullptr;
         }
     }
-    if (!conv_batch_build(b, best_lg)) {
+    if (!conv_batch_build(b, best_lg, best_class, best_small)) {
         destroy_conv_batch(b);
         return nullptr;
     }
@@ -2222,7 +2354,14 @@ int mufft_gb_conv_batch_status(mufft_gb_conv_batch *batch)
 
 unsigned mufft_gb_conv_batch_split_size(const mufft_gb_conv_batch *batch)
 {
-    return batch ? (batch->split_lg >= 17 ? 0u : 1u << batch->split_lg) : 0u;
+    if (!batch || batch->split_lg >= 17 || batch->split_lg >= batch->class_lg)
+        return 0u;
+    return 1u << batch->split_lg;
+}
+
+unsigned mufft_gb_conv_batch_class_size(const mufft_gb_conv_batch *batch)
+{
+    return batch ? (batch->class_lg >= 17 ? 0u : 1u << batch->class_lg) : 0u;
 }
 
 void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch) { destroy_conv_batch(batch); }
@@ -2980,6 +3119,16 @@ int mufft_gb_autotune_load(const char *path)
     std::lock_guard<std::mutex> lock(g_tune_mu);
     for (const auto &kv : loaded)
         g_tune[kv.first] = kv.second;
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_conv_classes(unsigned points)
+{
+    if (points != 0 && (!is_pow2(points) || points < (1u << kRaggedMinSplitLg) || points > 65536)) {
+        set_error(MUFFT_GB_ERR_INVALID, "class size must be 0 or a power of two in 16384..65536");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_conv_class_lg.store(points ? ilog2u(points) : 17u);
     return MUFFT_GB_OK;
 }
 

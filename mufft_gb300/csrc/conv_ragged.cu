@@ -318,6 +318,84 @@ size_t conv_ragged_smem()
     return m;
 }
 
+namespace {
+
+// Phase launches of class pipelines (see conv_ragged.h): F1 reads the request's
+// input, I2 writes its output, the others work on its spectrum scratch.
+template <int L, int C, int LMAP, int SMAP>
+__global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L, 16, C, 1>())
+    class_tile(const TileArgs tmpl, const ClassEntry *tab, int phase)
+{
+    extern __shared__ float2 smem[];
+    const ClassEntry e = tab[blockIdx.y];
+    TileArgs a = tmpl;
+    a.in = phase == 0 ? e.in : e.spec;
+    a.out = phase == 4 ? e.out : e.spec;
+    tile_body<L, 16, C, 1, LMAP, SMAP, false>(a, blockIdx.x, 0, 0, 0, smem);
+}
+
+// The multiply phase for a table of requests (blockIdx.y), on the transposed
+// spectrum X^T[k1][k2] = X[k1 + L1*k2] of L = L1 x L2 points, as
+// conv_multiply above.
+__global__ void __launch_bounds__(256) class_multiply(const ClassEntry *tab, unsigned l1, unsigned l2, int stereo,
+                                                      float scale, const float2 *rtw_fwd, const float2 *rtw_inv)
+{
+    const ClassEntry e = tab[blockIdx.y];
+    const int L1 = 1 << l1, L2 = 1 << l2, L = L1 * L2;
+    float2 *s = e.spec;
+    const int stride = gridDim.x * blockDim.x;
+    if (stereo) {
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < L; idx += stride) {
+            const int k = (idx >> l2) + L1 * (idx & (L2 - 1));
+            s[idx] = cscale(cmul(s[idx], __ldg(&e.h[k])), scale);
+        }
+        return;
+    }
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= L / 2; k += stride) {
+        if (k == 0) {
+            const float2 z0 = s[0];
+            const float2 x0 = make_float2(z0.x + z0.y, 0.f), xm = make_float2(z0.x - z0.y, 0.f);
+            const float2 y0 = cscale(cmul(x0, __ldg(&e.h[0])), scale);
+            const float2 ym = cscale(cmul(xm, __ldg(&e.h[L])), scale);
+            s[0] = c2r_fixup(y0, ym, __ldg(&rtw_inv[0]));
+            continue;
+        }
+        const int km = L - k;
+        const int ik = ((k & (L1 - 1)) << l2) + (k >> l1), im = ((km & (L1 - 1)) << l2) + (km >> l1);
+        const float2 zk = s[ik], zm = s[im];
+        float2 xk, xk_hi, xm, xm_hi;
+        r2c_bins(zk, zm, __ldg(&rtw_fwd[k]), xk, xk_hi);
+        r2c_bins(zm, zk, __ldg(&rtw_fwd[km]), xm, xm_hi);
+        const float2 yk = cscale(cmul(xk, __ldg(&e.h[k])), scale);
+        const float2 ym = cscale(cmul(xm, __ldg(&e.h[km])), scale);
+        s[ik] = c2r_fixup(yk, ym, __ldg(&rtw_inv[k]));
+        if (km != k)
+            s[im] = c2r_fixup(ym, yk, __ldg(&rtw_inv[km]));
+    }
+}
+
+}  // namespace
+
+ClassTile class_column_tile(int L1)
+{
+    if (L1 == 128)
+        return ClassTile{(const void *)&class_tile<128, 32, ACROSS, ACROSS>, 128, 32, tile_threads<128, 16, 32, 1>(),
+                         tile_smem_bytes<128, 16, 32, 1, ACROSS, ACROSS>()};
+    return ClassTile{(const void *)&class_tile<256, 16, ACROSS, ACROSS>, 256, 16, tile_threads<256, 16, 16, 1>(),
+                     tile_smem_bytes<256, 16, 16, 1, ACROSS, ACROSS>()};
+}
+
+ClassTile class_row_tile(int L2)
+{
+    if (L2 == 128)
+        return ClassTile{(const void *)&class_tile<128, 32, ALONG, ALONG>, 128, 32, tile_threads<128, 16, 32, 1>(),
+                         tile_smem_bytes<128, 16, 32, 1, ALONG, ALONG>()};
+    return ClassTile{(const void *)&class_tile<256, 16, ALONG, ALONG>, 256, 16, tile_threads<256, 16, 16, 1>(),
+                     tile_smem_bytes<256, 16, 16, 1, ALONG, ALONG>()};
+}
+
+const void *class_multiply_fn() { return (const void *)&class_multiply; }
+
 const void *conv_ragged_fn() { return (const void *)&conv_ragged_kernel; }
 int conv_ragged_threads() { return kThreads; }
 

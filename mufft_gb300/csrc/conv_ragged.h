@@ -51,4 +51,25 @@ const void *conv_ragged_fn();
 int conv_ragged_threads();
 size_t conv_ragged_smem();
 
+// Class pipelines: requests of one (size, method, zero-pad) class whose
+// five four-step phases run as ordinary batched launches over a table of the
+// requests' buffers (blockIdx.y picks the request).
+struct ClassEntry {
+    const float2 *in;
+    const float2 *h;
+    float2 *out;
+    float2 *spec;
+};
+
+struct ClassTile {
+    const void *fn;  // kernel(TileArgs tmpl, const ClassEntry *tab, int phase)
+    int L, C, threads;
+    size_t smem;     // with the twiddle region
+};
+// Phase 0/4 (columns of L1) and 1/3 (rows of L2) tiles for a split L1 x L2.
+ClassTile class_column_tile(int L1);
+ClassTile class_row_tile(int L2);
+const void *class_multiply_fn();  // kernel(const ClassEntry *tab, unsigned l1, unsigned l2, int stereo, float scale,
+                                  //        const float2 *rtw_fwd, const float2 *rtw_inv)
+
 }  // namespace mgb

@@ -184,6 +184,7 @@ def test_conv_batch_autotuned_split_size(gpu, ora, torch):
     try:
         split = gpu.gb_conv_batch_split_size(bt.handle)
         assert split in (0, 1 << 14, 1 << 15, 1 << 16)
+        assert gpu.gb_conv_batch_class_size(bt.handle) in (0, 1 << 14, 1 << 15, 1 << 16)
         outs = bt.run(torch)
     finally:
         bt.free()
@@ -200,9 +201,11 @@ def test_conv_batch_forced_split_sizes(gpu, ora, torch, split):
              (1 << 14, STEREO), (2048, 0), (64, STEREO)]
     try:
         assert gpu.gb_set_conv_split(split) == 0
+        assert gpu.gb_set_conv_classes(0) == 0
         bt = Batch(gpu, torch, specs, 95000 + split)
     finally:
         gpu.gb_set_conv_split(1 << 16)
+        gpu.gb_set_conv_classes(1 << 14)
     try:
         assert gpu.gb_conv_batch_split_size(bt.handle) == split
         outs = bt.run(torch)
@@ -210,3 +213,25 @@ def test_conv_batch_forced_split_sizes(gpu, ora, torch, split):
         bt.free()
     for i, ((N, method), got) in enumerate(zip(specs, outs)):
         assert rel_l2(got, ora.conv(bt.a[i], bt.b[i], N, method)) <= REL_L2_TOL, (i, N, method, split)
+
+
+@pytest.mark.parametrize("classes", [1 << 14, 1 << 15, 1 << 16])
+def test_conv_batch_class_pipelines(gpu, ora, torch, classes):
+    """Large requests as class pipelines (batched launches per size class on
+    parallel graph branches) beside the persistent kernel."""
+    specs = [(1 << 17, 0), (1 << 16, STEREO), (1 << 15, PAD1), (1 << 15, STEREO | PAD1), (1 << 16, PAD1 | PAD2),
+             (1 << 14, STEREO), (1 << 17, PAD1), (1 << 16, STEREO), (2048, 0), (64, STEREO)]
+    try:
+        assert gpu.gb_set_conv_classes(classes) == 0
+        bt = Batch(gpu, torch, specs, 96000 + classes)
+    finally:
+        gpu.gb_set_conv_classes(1 << 14)
+    try:
+        assert gpu.gb_conv_batch_class_size(bt.handle) == classes
+        outs = bt.run(torch)
+        again = bt.run(torch)
+    finally:
+        bt.free()
+    for i, ((N, method), got) in enumerate(zip(specs, outs)):
+        assert rel_l2(got, ora.conv(bt.a[i], bt.b[i], N, method)) <= REL_L2_TOL, (i, N, method, classes)
+        assert np.array_equal(got.view(np.uint32), again[i].view(np.uint32))
