@@ -465,18 +465,29 @@ def companion_stream_conv(lib, torch) -> dict:
     block, taps = 1024, 1 << 20
     t = np.arange(taps)
     h = (signals.normal(7, taps) * np.exp(-t / 8192.0)).astype(np.float32)
-    conv = lib.gb_create_stream_conv(block, 1, h.ctypes.data, taps, 0)
-    if not conv:
-        raise RuntimeError(lib.gb_last_error_string().decode())
     sp = torch.cuda.current_stream().cuda_stream
-    ms = _time_ms(torch, lambda: lib.gb_stream_conv_process(conv, sp), reps=200, warm=20)
-    lib.gb_free_stream_conv(conv)
+    res = {}
+    for fused in (1, 0):
+        lib.gb_set_stream_conv_fused(fused)
+        conv = lib.gb_create_stream_conv(block, 1, h.ctypes.data, taps, 0)
+        lib.gb_set_stream_conv_fused(1)
+        if not conv:
+            raise RuntimeError(lib.gb_last_error_string().decode())
+        res[fused] = (_time_ms(torch, lambda: lib.gb_stream_conv_process(conv, sp), reps=200, warm=20),
+                      lib.gb_stream_conv_fused(conv), lib.gb_stream_conv_ranges(conv))
+        if lib.gb_stream_conv_status(conv) != 0:
+            raise RuntimeError(lib.gb_last_error_string().decode())
+        lib.gb_free_stream_conv(conv)
+    ms, fused, ranges = res[1]
     P = taps // block
     mac_bytes = 2.0 * P * (2 * block) * 8  # filter spectra + delay line, every block
     return {"workload": "stereo stream, 1024-frame blocks, 2^20-tap filter (1024 uniform partitions)",
             "ms_per_block": ms, "frames_per_s": block / (ms * 1e-3),
             "realtime_factor_48khz": (block / 48000.0) / (ms * 1e-3),
-            "mac_GB/s": mac_bytes / (ms * 1e-3) / 1e9}
+            "mac_GB/s": mac_bytes / (ms * 1e-3) / 1e9,
+            "launch": "one fused launch per block" if fused else "graph of separate launches",
+            "partition_ranges": ranges,
+            "graph_of_launches_ms_per_block": res[0][0]}
 
 
 def companion_split(lib, torch) -> dict:

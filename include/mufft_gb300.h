@@ -204,6 +204,23 @@ int mufft_gb_stream_conv_process(mufft_gb_stream_conv *conv, void *stream);
 /* Forgets the input history (as if the stream restarted from silence). */
 int mufft_gb_stream_conv_reset(mufft_gb_stream_conv *conv, void *stream);
 void mufft_gb_free_stream_conv(mufft_gb_stream_conv *conv);
+/* Partition ranges the multiply-accumulate of convolvers created afterwards
+ * splits the P partitions into (each range a row of CTAs whose partial sums
+ * are added in range order); 0, the default, sizes it to the GPU.  Values
+ * above P are clamped to P. */
+int mufft_gb_set_stream_conv_ranges(unsigned ranges);
+/* Partition ranges a convolver uses. */
+unsigned mufft_gb_stream_conv_ranges(const mufft_gb_stream_conv *conv);
+/* Convolvers created afterwards whose windows one 256-thread row tile
+ * transforms (64 .. 4096 complex points) run a block as one launch -- the
+ * forward transform, the multiply-accumulate and the inverse transform in
+ * one grid, ordered by tickets (1, default) -- or as a graph of separate
+ * launches (0).  mufft_gb_stream_conv_fused reports which a convolver uses. */
+int mufft_gb_set_stream_conv_fused(int enable);
+int mufft_gb_stream_conv_fused(const mufft_gb_stream_conv *conv);
+/* Synchronises the device; nonzero if a block launch's bounded wait timed
+ * out since the last call (its output block is then not valid). */
+int mufft_gb_stream_conv_status(mufft_gb_stream_conv *conv);
 
 /* ------------------------------------------------- allocation-free execute */
 
@@ -288,6 +305,15 @@ int mufft_gb_set_2d_columns(int mode);
  * persistent CTAs (1) or single-buffered (2), or load it with per-thread
  * loads (0, default). */
 int mufft_gb_set_tma(int mode);
+/* Tile passes of plans created afterwards run at most `ctas_per_sm` CTAs per
+ * SM (they request the matching share of shared memory); 0, the default, lets
+ * as many run as fit.  A grid that fills the GPU about once then runs in
+ * several waves, and CTAs loading their inputs overlap CTAs storing results. */
+int mufft_gb_set_tile_occupancy(int ctas_per_sm);
+/* Contiguous row passes (batched 1D transforms, 2D rows) of plans created
+ * afterwards run as persistent CTAs that prefetch their next tile's inputs
+ * while they transform the current one (1), or as one CTA per tile (0). */
+int mufft_gb_set_stream_tiles(int enable);
 /* Split-precision plans (MUFFT_GB_FLAG_SPLIT_*) created afterwards run their
  * products on tcgen05.mma with TMEM accumulators (0, default) or on
  * warp-level mma.sync (1). */

@@ -93,6 +93,8 @@ GB_H = [
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
     ("set_split_engine", _i, [_i]),
     ("set_tma", _i, [_i]),
+    ("set_tile_occupancy", _i, [_i]),
+    ("set_stream_tiles", _i, [_i]),
     ("set_2d_columns", _i, [_i]),
     ("autotune_1d", _i, [_i, _u, _i, _u, _u, _vp, _sz]),
     ("autotune_save", _i, [C.c_char_p]),
@@ -103,6 +105,11 @@ GB_H = [
     ("stream_conv_output", _vp, [_vp]),
     ("stream_conv_process", _i, [_vp, _vp]),
     ("stream_conv_reset", _i, [_vp, _vp]),
+    ("set_stream_conv_ranges", _i, [_u]),
+    ("stream_conv_ranges", _u, [_vp]),
+    ("set_stream_conv_fused", _i, [_i]),
+    ("stream_conv_fused", _i, [_vp]),
+    ("stream_conv_status", _i, [_vp]),
     ("free_stream_conv", None, [_vp]),
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),

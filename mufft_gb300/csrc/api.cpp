@@ -37,6 +37,8 @@
 #include "misc_kernels.h"
 #include "split_tc.h"
 #include "tiles_tma.h"
+#include "tiles_stream.h"
+#include "stream_conv.h"
 #include "registry.h"
 
 using namespace mgb;
@@ -131,13 +133,31 @@ static const TmaTileKernel *find_tma(int L, int R, int C, int nbuf)
     return nullptr;
 }
 
+static std::vector<StreamTileKernel> &stream_table()
+{
+    static std::vector<StreamTileKernel> t = [] {
+        std::vector<StreamTileKernel> v;
+        register_tiles_stream(v);
+        return v;
+    }();
+    return t;
+}
+
+static const StreamTileKernel *find_stream(int L, int R, int C)
+{
+    for (const StreamTileKernel &k : stream_table())
+        if (k.L == L && k.R == R && k.C == C)
+            return &k;
+    return nullptr;
+}
+
 static std::mutex g_choice_mu;
 static std::vector<TileKernel> g_choice;  // preferred (L, lmap, smap) -> C
 
 // Schedule choices of one plan (the autotuner's unit): -2 leaves a knob at its
 // process-wide setting; `tiles` are preferred (L, lmap, smap) -> (C, R, Q).
 struct PlanOptions {
-    int levels = -2, twiddle = -2, fused = -2, tma = -2;
+    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2;
     std::vector<TileKernel> tiles;
 };
 // Set while a plan is built with explicit choices (candidate or remembered).
@@ -327,6 +347,13 @@ struct Pass {
     SplitArgs sp{};
     int sp_stages = 0, sp_limbs = 0, sp_engine = 0;
     unsigned sp_grid = 0;
+    // resident-CTA cap: tile launches request at least this much dynamic
+    // shared memory (0: the kernel's own need)
+    size_t smem_min = 0;
+    // row tiles as persistent CTAs streaming their tiles (tiles_stream.cu);
+    // `k` is the same tile as one launch per tile
+    const StreamTileKernel *sk = nullptr;
+    unsigned sk_grid = 0;
 };
 
 struct Buffers {
@@ -423,8 +450,17 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                     continue;
                 }
             }
+            if (p.sk) {
+                unsigned ntiles = p.grid.x;
+                void *sargs[] = {&a, &ntiles};
+                cudaError_t e = cudaLaunchKernel(p.sk->fn, dim3(p.sk_grid), dim3(p.sk->threads), sargs, p.sk->smem, st);
+                if (e != cudaSuccess)
+                    return e;
+                continue;
+            }
             void *args[] = {&a};
-            const size_t smem = (a.tw_lo || a.tw_colpow || a.tw_by_y) ? p.k->smem : p.k->smem_ex;
+            const size_t smem =
+                std::max((a.tw_lo || a.tw_colpow || a.tw_by_y) ? p.k->smem : p.k->smem_ex, p.smem_min);
             cudaError_t e;
             if (p.k->Q > 1) {
                 // one tile per cluster of Q CTAs (distributed shared memory)
@@ -501,8 +537,8 @@ std::string describe(const std::vector<Pass> &ps)
         const Pass &p = ps[i];
         if (p.type == PASS_TILE)
             snprintf(buf, sizeof(buf), "%stile%s L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s%s conj=%d",
-                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : "", p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
-                     p.k->smap ? "across" : "along", p.grid.x, p.grid.y, p.k->threads, p.k->smem,
+                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? "+stream" : ""), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
+                     p.k->smap ? "across" : "along", p.sk ? p.sk_grid : p.grid.x, p.grid.y, p.k->threads, std::max(p.k->smem, p.smem_min),
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
                      p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
                      p.a.conj);
@@ -600,6 +636,14 @@ int opt_tma() { return (t_opts && t_opts->tma != -2) ? t_opts->tma : g_tma.load(
 int opt_twiddle() { return (t_opts && t_opts->twiddle != -2) ? t_opts->twiddle : g_twiddle_table.load(); }
 int opt_levels() { return (t_opts && t_opts->levels != -2) ? t_opts->levels : g_levels.load(); }
 int opt_fused() { return (t_opts && t_opts->fused != -2) ? t_opts->fused : g_fused_bc.load(); }
+// Resident tile CTAs per SM (0: as many as fit).  A cap spreads a grid that
+// would fill the GPU about once over several waves, so that CTAs loading
+// their inputs overlap CTAs storing their outputs.
+std::atomic<int> g_occ{0};
+int opt_occ() { return (t_opts && t_opts->occ != -2) ? t_opts->occ : g_occ.load(); }
+// Row tiles of one launch per tile (0) or persistent streaming CTAs (1).
+std::atomic<int> g_stream{0};
+int opt_stream() { return (t_opts && t_opts->stream != -2) ? t_opts->stream : g_stream.load(); }
 
 bool use_twiddle_table(const TileKernel *k)
 {
@@ -679,6 +723,67 @@ bool attach_tma(std::vector<Pass> &ps, PlanResources &res, bool dry, int device)
                          !cuda_ok(cudaMemset(res.err, 0, sizeof(int)), "cudaMemset(err)")))
             return false;
         p.tma_err = res.err;
+    }
+    return true;
+}
+
+// Gives every contiguous row-tile pass (one batch dimension, unit strides)
+// that has a streaming variant that variant: a persistent grid of SMs x
+// resident CTAs whose CTAs prefetch their next tile's inputs.
+bool attach_stream(std::vector<Pass> &ps, bool dry, int device)
+{
+    if (opt_stream() != 1)
+        return true;
+    for (Pass &p : ps) {
+        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.k->lmap != ALONG || p.k->smap != ALONG || p.tk ||
+            p.grid.y != 1 || p.a.ysplit || p.a.in_stride != 1 || p.a.out_stride != 1)
+            continue;
+        const StreamTileKernel *sk = find_stream(p.k->L, p.k->R, p.k->C);
+        if (!sk)
+            continue;
+        int sms = 152, per_sm = 1;
+        if (!dry) {
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (sk->smem > 48 * 1024 &&
+                !cuda_ok(cudaFuncSetAttribute(sk->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sk->smem),
+                         "cudaFuncSetAttribute(stream)"))
+                return false;
+            if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sk->fn, sk->threads, sk->smem),
+                         "occupancy(stream)"))
+                return false;
+        }
+        p.sk = sk;
+        p.sk_grid = std::min(p.grid.x, (unsigned)(sms * std::max(per_sm, 1)));
+    }
+    return true;
+}
+
+// Applies the resident-CTA cap to every single-CTA tile pass: the launch
+// asks for enough dynamic shared memory that at most `occ` CTAs fit per SM.
+bool attach_occupancy(std::vector<Pass> &ps, bool dry, int device)
+{
+    const int occ = opt_occ();
+    if (occ <= 0)
+        return true;
+    int per_sm = 233472, optin = 232448;
+    if (!dry) {
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    }
+    // each resident CTA also takes 1 KiB of reserved shared memory
+    const int w = std::min(per_sm / occ - 1024, optin);
+    if (w <= 0)
+        return true;
+    const size_t want = (size_t)w & ~(size_t)127;
+    for (Pass &p : ps) {
+        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.tk || p.sk)
+            continue;
+        if (want <= p.k->smem)
+            continue;
+        p.smem_min = want;
+        if (!dry && !cuda_ok(cudaFuncSetAttribute(p.k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
+                             "cudaFuncSetAttribute(occupancy)"))
+            return false;
     }
     return true;
 }
@@ -1281,7 +1386,9 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
                 t_opts = &tuned;
         }
         const bool built = build_fft_passes(s, tw, pl->res, dry, pl->passes) &&
-                           attach_tma(pl->passes, pl->res, dry, pl->device);
+                           attach_tma(pl->passes, pl->res, dry, pl->device) &&
+                           attach_stream(pl->passes, dry, pl->device) &&
+                           attach_occupancy(pl->passes, dry, pl->device);
         t_opts = prev;
         if (!built) {
             destroy_1d(pl);
@@ -2370,20 +2477,26 @@ void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch) { destroy_conv_batch(b
 
 // ======================================================= streaming convolution
 
+static std::atomic<unsigned> g_stream_ranges{0};
+static std::atomic<int> g_stream_fused{1};
+
 struct mufft_gb_stream_conv {
     int device = -1;
-    unsigned block = 0, P = 0, nb = 0;
+    unsigned block = 0, P = 0, nb = 0, pitch = 0;
     bool stereo = false;
     mufft_plan_1d *fwd = nullptr, *inv = nullptr;
     void *win = nullptr;      // 2 x block samples: previous block, then the caller's input
     float2 *xcur = nullptr;   // spectrum of the current window (nb bins)
-    float2 *fdl = nullptr;    // P x nb: spectra of the last P windows
-    float2 *h = nullptr;      // P x nb: filter-partition spectra
+    float2 *fdl = nullptr;    // P rows of `pitch` bins: spectra of the last P windows
+    float2 *h = nullptr;      // P rows of `pitch` bins: filter-partition spectra
     float2 *y = nullptr;      // nb bins of the output spectrum
     void *ybuf = nullptr;     // 2 x block samples of the inverse; the output is the second half
-    float2 *part = nullptr;   // G x nb partial sums of the multiply-accumulate
-    unsigned G = 1;           // partition ranges per bin column
-    unsigned *counter = nullptr;  // [0] blocks processed, [1] CTA ticket, [2 + x] bin-column tickets
+    float2 *part = nullptr;   // G rows of `pitch` bins: partial sums of the multiply-accumulate
+    unsigned G = 1;           // partition ranges per bin group
+    int M = 0;                // nonzero: one fused launch per block, row tiles of M points
+    int *err = nullptr;       // a bounded wait of the fused launch timed out
+    UpolsBlockArgs block_args{};
+    unsigned *counter = nullptr;  // [0] blocks processed, [1] CTA ticket, [2 + x] bin-group tickets
     size_t counter_bytes = 0;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -2411,6 +2524,7 @@ void destroy_stream_conv(mufft_gb_stream_conv *c)
         cudaFree(c->ybuf);
         cudaFree(c->part);
         cudaFree(c->counter);
+        cudaFree(c->err);
     }
     delete c;
 }
@@ -2431,11 +2545,13 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
     const unsigned L = 2 * block;
     const unsigned P = (taps + block - 1) / block;
     const unsigned nb = stereo ? L : block + 1;
+    const unsigned pitch = upols_pitch(nb);
     const unsigned tflags = flags & ~(unsigned)(MUFFT_FLAG_ZERO_PAD_UPPER_HALF | MUFFT_FLAG_FULL_R2C);
     mufft_gb_stream_conv *c = new mufft_gb_stream_conv();
     c->block = block;
     c->P = P;
     c->nb = nb;
+    c->pitch = pitch;
     c->stereo = stereo;
     c->fwd = create_1d(stereo ? K_C2C : K_R2C, L, MUFFT_FORWARD, tflags, 1, 0, 0, -1, false, nullptr);
     c->inv = create_1d(stereo ? K_C2C : K_C2R, L, MUFFT_INVERSE, tflags, 1, 0, 0, -1, false, nullptr);
@@ -2448,24 +2564,55 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
     const size_t sample = stereo ? sizeof(float2) : sizeof(float);
     // filter partitions: P zero-padded windows of L reals, transformed as one batch
     mufft_plan_1d *hp = create_1d(K_R2C, L, MUFFT_FORWARD, tflags | (stereo ? MUFFT_FLAG_FULL_R2C : 0), P,
-                                  L, nb, -1, false, nullptr);
+                                  L, pitch, -1, false, nullptr);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    c->G = upols_chunks(nb, P, sms);
-    c->counter_bytes = (2 + (nb + 255) / 256) * sizeof(unsigned);
+    const unsigned want_ranges = g_stream_ranges.load();
+    // One launch per block when both transforms are one 256-thread row tile
+    const unsigned M = stereo ? L : L / 2;
+    auto row_tile = [M](const mufft_plan_1d *pl) {
+        if (pl->passes.size() != 1)
+            return false;
+        const Pass &p = pl->passes[0];
+        return p.type == PASS_TILE && p.k && !p.tk && !p.sk && p.smem_min == 0 && p.k->Q == 1 && p.k->R == 16 &&
+               p.k->lmap == ALONG && p.k->smap == ALONG && p.k->L == (int)M && p.k->C * p.k->L == 4096 &&
+               p.grid.x == 1 && p.grid.y == 1 && p.in_role == ROLE_IN && p.out_role == ROLE_OUT;
+    };
+    if (g_stream_fused.load() && upols_block_supported((int)M) && row_tile(c->fwd) && row_tile(c->inv)) {
+        int per_sm = 0;
+        if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, upols_block_fn((int)M), 256,
+                                                                   upols_block_smem((int)M)),
+                     "occupancy(stream convolution)")) {
+            destroy_stream_conv(c);
+            return nullptr;
+        }
+        c->M = (int)M;
+        // partitions 1 .. P-1 over ranges (at least one range CTA per group:
+        // it finishes the group); all CTAs resident at once
+        const unsigned slots = (unsigned)std::max(2, sms * std::max(per_sm, 1));
+        const unsigned max_g = std::max(1u, (slots - 1) / upols_groups(nb));
+        c->G = std::max(1u, std::min({want_ranges ? want_ranges : max_g, max_g, std::max(P - 1, 1u)}));
+    } else {
+        c->G = want_ranges ? std::min(want_ranges, P) : upols_chunks(nb, P, sms);
+    }
+    c->counter_bytes = (c->M ? upols_block_tickets(upols_groups(nb)) : 2 + upols_groups(nb)) * sizeof(unsigned);
     float *hpad = nullptr;
     bool ok = hp && cuda_ok(cudaMalloc(&c->win, 2 * (size_t)block * sample), "cudaMalloc(window)") &&
               cuda_ok(cudaMalloc(&c->xcur, (size_t)nb * sizeof(float2)), "cudaMalloc(spectrum)") &&
-              cuda_ok(cudaMalloc(&c->fdl, (size_t)P * nb * sizeof(float2)), "cudaMalloc(delay line)") &&
-              cuda_ok(cudaMalloc(&c->h, (size_t)P * nb * sizeof(float2)), "cudaMalloc(filter spectra)") &&
+              cuda_ok(cudaMalloc(&c->fdl, (size_t)P * pitch * sizeof(float2)), "cudaMalloc(delay line)") &&
+              cuda_ok(cudaMalloc(&c->h, (size_t)P * pitch * sizeof(float2)), "cudaMalloc(filter spectra)") &&
+              cuda_ok(cudaMemset(c->h, 0, (size_t)P * pitch * sizeof(float2)), "cudaMemset") &&
               cuda_ok(cudaMalloc(&c->y, (size_t)nb * sizeof(float2)), "cudaMalloc(output spectrum)") &&
               cuda_ok(cudaMalloc(&c->ybuf, 2 * (size_t)block * sample), "cudaMalloc(output)") &&
-              cuda_ok(cudaMalloc(&c->part, (size_t)c->G * nb * sizeof(float2)), "cudaMalloc(partials)") &&
+              cuda_ok(cudaMalloc(&c->part, (size_t)std::max(c->G, 1u) * pitch * sizeof(float2)),
+                      "cudaMalloc(partials)") &&
               cuda_ok(cudaMalloc(&c->counter, c->counter_bytes), "cudaMalloc(counter)") &&
+              cuda_ok(cudaMalloc(&c->err, sizeof(int)), "cudaMalloc(err)") &&
+              cuda_ok(cudaMemset(c->err, 0, sizeof(int)), "cudaMemset") &&
               cuda_ok(cudaMalloc(&hpad, (size_t)P * L * sizeof(float)), "cudaMalloc(partitions)") &&
               cuda_ok(cudaMemset(hpad, 0, (size_t)P * L * sizeof(float)), "cudaMemset") &&
               cuda_ok(cudaMemset(c->win, 0, 2 * (size_t)block * sample), "cudaMemset") &&
-              cuda_ok(cudaMemset(c->fdl, 0, (size_t)P * nb * sizeof(float2)), "cudaMemset") &&
+              cuda_ok(cudaMemset(c->fdl, 0, (size_t)P * pitch * sizeof(float2)), "cudaMemset") &&
               cuda_ok(cudaMemset(c->counter, 0, c->counter_bytes), "cudaMemset");
     // partition p = filter[p*block .. (p+1)*block) at the start of window p
     for (unsigned p = 0; ok && p < P; p++) {
@@ -2482,7 +2629,35 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
         return nullptr;
     }
     // one block: spectrum of [previous, input], multiply-accumulate, inverse,
-    // then the input becomes the previous block
+    // then the input becomes the previous block -- one fused launch, or a
+    // graph of the separate launches
+    if (c->M) {
+        UpolsBlockArgs &a = c->block_args;
+        a.fwd = c->fwd->passes[0].a;
+        a.fwd.in = (const float2 *)c->win;
+        a.fwd.out = c->xcur;
+        a.fwd.in2 = nullptr;
+        a.inv = c->inv->passes[0].a;
+        a.inv.in = c->y;
+        a.inv.out = (float2 *)c->ybuf;
+        a.inv.in2 = nullptr;
+        a.xcur = c->xcur;
+        a.fdl = c->fdl;
+        a.h = c->h;
+        a.part = c->part;
+        a.y = c->y;
+        a.win = (float4 *)c->win;
+        a.half16 = (unsigned)((size_t)block * sample / 16);
+        a.nb = nb;
+        a.pitch = pitch;
+        a.P = P;
+        a.G = c->G;
+        a.groups = upols_groups(nb);
+        a.tickets = c->counter;
+        a.err = c->err;
+        a.s = 1.0f / (float)L;
+        return c;
+    }
     cudaGraph_t gr = nullptr;
     ok = cuda_ok(cudaStreamCreateWithFlags(&c->capture, cudaStreamNonBlocking), "cudaStreamCreate") &&
          cuda_ok(cudaStreamBeginCapture(c->capture, cudaStreamCaptureModeThreadLocal), "capture");
@@ -2528,6 +2703,12 @@ int mufft_gb_stream_conv_process(mufft_gb_stream_conv *c, void *stream)
         return MUFFT_GB_ERR_INVALID;
     }
     DeviceGuard g(c->device);
+    if (c->M) {
+        // one kernel: launched directly (a graph launch adds latency)
+        if (!cuda_ok(launch_upols_block(c->M, c->block_args, (cudaStream_t)stream), "block launch"))
+            return t_err;
+        return MUFFT_GB_OK;
+    }
     if (!cuda_ok(cudaGraphLaunch(c->exec, (cudaStream_t)stream), "cudaGraphLaunch"))
         return t_err;
     return MUFFT_GB_OK;
@@ -2543,13 +2724,56 @@ int mufft_gb_stream_conv_reset(mufft_gb_stream_conv *c, void *stream)
     const cudaStream_t st = (cudaStream_t)stream;
     const size_t sample = c->stereo ? sizeof(float2) : sizeof(float);
     if (!cuda_ok(cudaMemsetAsync(c->win, 0, 2 * (size_t)c->block * sample, st), "reset") ||
-        !cuda_ok(cudaMemsetAsync(c->fdl, 0, (size_t)c->P * c->nb * sizeof(float2), st), "reset") ||
+        !cuda_ok(cudaMemsetAsync(c->fdl, 0, (size_t)c->P * c->pitch * sizeof(float2), st), "reset") ||
         !cuda_ok(cudaMemsetAsync(c->counter, 0, c->counter_bytes, st), "reset"))
         return t_err;
     return MUFFT_GB_OK;
 }
 
 void mufft_gb_free_stream_conv(mufft_gb_stream_conv *c) { destroy_stream_conv(c); }
+
+int mufft_gb_set_stream_conv_ranges(unsigned ranges)
+{
+    if (ranges > (1u << 20)) {
+        set_error(MUFFT_GB_ERR_INVALID, "at most 2^20 partition ranges");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_stream_ranges.store(ranges);
+    return MUFFT_GB_OK;
+}
+
+unsigned mufft_gb_stream_conv_ranges(const mufft_gb_stream_conv *c) { return c ? c->G : 0u; }
+
+int mufft_gb_set_stream_conv_fused(int enable)
+{
+    if (enable < 0 || enable > 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "enable must be 0 or 1");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_stream_fused.store(enable);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_stream_conv_fused(const mufft_gb_stream_conv *c) { return c && c->M ? 1 : 0; }
+
+int mufft_gb_stream_conv_status(mufft_gb_stream_conv *c)
+{
+    if (!c) {
+        set_error(MUFFT_GB_ERR_INVALID, "null convolver");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    DeviceGuard g(c->device);
+    int e = 0;
+    if (!cuda_ok(cudaDeviceSynchronize(), "synchronize") ||
+        !cuda_ok(cudaMemcpy(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost), "error flag"))
+        return t_err;
+    if (e) {
+        cudaMemset(c->err, 0, sizeof(int));
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "a bounded wait in the block launch timed out");
+        return MUFFT_GB_ERR_UNSUPPORTED;
+    }
+    return MUFFT_GB_OK;
+}
 
 }  // extern "C"
 
@@ -2692,7 +2916,9 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         // columns first into scratch (Nx/2 + 1 of them), then rows with the
         // fused c2r fix-up (fft.c:863-916)
         pl->vertical_nx = Mx + 1;
-        const size_t sstride = Mx + 1;
+        // rows of the Mx + 1 columns at a pitch of whole 128-byte lines: the
+        // column tiles then store full sectors
+        const size_t sstride = ((size_t)Mx + 1 + 15) & ~(size_t)15;
         pl->res.scratch_bytes = sstride * Ny * sizeof(float2);
         if (!cuda_ok(cudaMalloc(&pl->res.scratch, pl->res.scratch_bytes), "cudaMalloc(scratch)")) {
             destroy_2d(pl);
@@ -2733,7 +2959,7 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
     if ((mode == 2 || (mode == 0 && Ny >= 8192)) && N1 >= 2 && kc1 && kc2) {
         const unsigned ncols = (unsigned)col.a.ntrans;
         const long long s_in = col.a.in_stride;                                 // pitch the columns are read at
-        const long long s_out = kind == K2_C2R ? (long long)(Mx + 1) : (long long)Nx;  // pitch of C1 / C2 outputs
+        const long long s_out = kind == K2_C2R ? col.a.out_stride : (long long)Nx;  // pitch of C1 / C2 outputs
         const Role c1_in = kind == K2_C2R ? ROLE_IN : ROLE_SCRATCH;
         const Role c1_out = ROLE_SCRATCH;
         const Role c2_out = kind == K2_C2R ? ROLE_SCRATCH2 : ROLE_OUT;
@@ -2790,14 +3016,16 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
             pl->passes.push_back(c1);
             pl->passes.push_back(c2);
         }
-        return pl;
-    }
-    if (kind == K2_C2R) {
+    } else if (kind == K2_C2R) {
         pl->passes.push_back(col);
         pl->passes.push_back(row);
     } else {
         pl->passes.push_back(row);
         pl->passes.push_back(col);
+    }
+    if (!attach_stream(pl->passes, false, pl->device) || !attach_occupancy(pl->passes, false, pl->device)) {
+        destroy_2d(pl);
+        return nullptr;
     }
     return pl;
 }
@@ -3159,6 +3387,26 @@ int mufft_gb_set_tma(int mode)
         return MUFFT_GB_ERR_INVALID;
     }
     g_tma.store(mode);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_stream_tiles(int enable)
+{
+    if (enable < 0 || enable > 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "enable must be 0 or 1");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_stream.store(enable);
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_set_tile_occupancy(int ctas_per_sm)
+{
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) {
+        set_error(MUFFT_GB_ERR_INVALID, "CTAs per SM must be 0 (no cap) .. 32");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    g_occ.store(ctas_per_sm);
     return MUFFT_GB_OK;
 }
 

@@ -561,9 +561,11 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // transforms tile*C .. tile*C + C - 1; ioff / ooff shift the input / output
 // base (batches); j is the CTA's rank in its cluster.  COH: load with
 // L2-coherent loads (input written earlier in the same launch).
-template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false>
+// PRE: the stage-0 registers were loaded by the caller (`pre`, R values).
+template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false, bool PRE = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
-                                          float2 *smem, const float2 *sin = nullptr, unsigned twy = 0)
+                                          float2 *smem, const float2 *sin = nullptr, unsigned twy = 0,
+                                          const float2 *pre = nullptr)
 {
     using S = Sched<L, R>;
     using TT = Tile<L, R, Q>;
@@ -610,7 +612,11 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     float2 v[R];
     int c, tl;
     split_tid<LMAP, C, TL>(threadIdx.x, c, tl);
-    if constexpr (SIN) {
+    if constexpr (PRE) {
+#pragma unroll
+        for (int q = 0; q < R; q++)
+            v[q] = pre[q];
+    } else if constexpr (SIN) {
         static_assert(Q == 1 && LMAP == ACROSS, "staged inputs are column tiles");
         load_stage0_sin<L, R, C>(a, sin, tile0 + c, c, tl, v);
     } else {

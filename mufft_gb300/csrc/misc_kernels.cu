@@ -88,63 +88,105 @@ __global__ void adjoint_filter_reduce(float2 *acc, const float2 *__restrict__ g,
 // Uniformly partitioned overlap-save, one block k: multiply-accumulate of
 // the current input spectrum and the previous P-1 ones (a ring of P slots,
 // block j in slot j % P) with the P filter-partition spectra, scaled; the
-// current spectrum then replaces block k-P in the ring.  CTAs tile
-// (256 bins) x (a range of partitions) so that long filters spread over the
-// whole GPU; each writes a partial sum, and the last CTA of a bin column
-// (ticket) adds the partials in partition order (deterministic).  The last
+// current spectrum then replaces block k-P in the ring.  Ring and filter
+// rows have a pitch of whole 64-bin groups (pad bins zero).  A CTA covers 64
+// bins (two per lane, 16-byte loads) and a range of partitions, which its 8
+// warps split round-robin; the warps' sums are added in shared memory in
+// warp order and written as the CTA's partial.  The last CTA of a bin group
+// (ticket) adds the partials in range order (deterministic), and the last
 // CTA overall advances the block counter.  Tickets never wait.
-//   tickets[0] = k, tickets[1] = CTAs done, tickets[2 + x] = column x done.
-__global__ void upols_mac(float2 *__restrict__ y, const float2 *__restrict__ xcur, float2 *fdl,
-                          const float2 *__restrict__ h, float2 *part, unsigned nb, unsigned P, unsigned *tickets,
-                          float s)
+//   tickets[0] = k, tickets[1] = CTAs done, tickets[2 + x] = bin group x done.
+constexpr int kMacWarps = 8;
+constexpr unsigned kMacBins = 64;
+
+__device__ __forceinline__ void cmac2(float4 &acc, const float4 a, const float4 b)
 {
+    acc.x += a.x * b.x - a.y * b.y;
+    acc.y += a.x * b.y + a.y * b.x;
+    acc.z += a.z * b.z - a.w * b.w;
+    acc.w += a.z * b.w + a.w * b.z;
+}
+
+__device__ __forceinline__ float4 add4(float4 a, const float4 b)
+{
+    a.x += b.x;
+    a.y += b.y;
+    a.z += b.z;
+    a.w += b.w;
+    return a;
+}
+
+__global__ void __launch_bounds__(kMacWarps * 32) upols_mac(float2 *__restrict__ y, const float2 *__restrict__ xcur,
+                                                            float2 *fdl, const float2 *__restrict__ h, float2 *part,
+                                                            unsigned nb, unsigned pitch, unsigned P,
+                                                            unsigned *tickets, float s)
+{
+    __shared__ float4 red[kMacWarps][32];
     __shared__ unsigned s_last;
     const unsigned k = *(volatile unsigned *)&tickets[0];
     const unsigned cur = k % P;
     const unsigned G = gridDim.y, g = blockIdx.y;
     const unsigned p0 = (unsigned)((unsigned long long)P * g / G), p1 = (unsigned)((unsigned long long)P * (g + 1) / G);
-    const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nb) {
-        const float2 x = xcur[b];
-        float2 acc = make_float2(0.f, 0.f);
-        unsigned slot = (cur + P - p0 % P) % P;  // slot of block k - p0
-        // unrolled so that several partitions' loads are in flight at once
-#pragma unroll 4
-        for (unsigned p = p0; p < p1; p++) {
-            const float2 xp = p == 0 ? x : __ldcg(&fdl[(size_t)slot * nb + b]);
-            const float2 hp = __ldg(&h[(size_t)p * nb + b]);
-            acc.x += xp.x * hp.x - xp.y * hp.y;
-            acc.y += xp.x * hp.y + xp.y * hp.x;
-            slot = slot ? slot - 1 : P - 1;  // block k - p - 1
-        }
-        part[(size_t)g * nb + b] = acc;
-        if (g == 0)
-            fdl[(size_t)cur * nb + b] = x;  // slot of block k - P: no CTA reads it for block k
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned b = blockIdx.x * kMacBins + 2 * lane;  // bins b, b + 1 (b < pitch, pitch even)
+    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (b + 1 < nb) {
+        const float2 x0 = xcur[b], x1 = xcur[b + 1];
+        x = make_float4(x0.x, x0.y, x1.x, x1.y);
+    } else if (b < nb) {
+        const float2 x0 = xcur[b];
+        x = make_float4(x0.x, x0.y, 0.f, 0.f);
     }
-    __threadfence();
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    // several partitions' loads in flight at once
+#pragma unroll 8
+    for (unsigned p = p0 + w; p < p1; p += kMacWarps) {
+        const unsigned slot = cur >= p ? cur - p : cur + P - p;  // block k - p
+        const float4 xp = p == 0 ? x : __ldg((const float4 *)&fdl[(size_t)slot * pitch + b]);
+        const float4 hp = __ldg((const float4 *)&h[(size_t)p * pitch + b]);
+        cmac2(acc, xp, hp);
+    }
+    red[w][lane] = acc;
+    __syncthreads();
+    if (w == 0) {
+        float4 t = red[0][lane];
+#pragma unroll
+        for (int q = 1; q < kMacWarps; q++)
+            t = add4(t, red[q][lane]);
+        *(float4 *)&part[(size_t)g * pitch + b] = t;
+        if (g == 0)
+            *(float4 *)&fdl[(size_t)cur * pitch + b] = x;  // slot of block k - P: no CTA reads it for block k
+        __threadfence();  // the writers' stores are visible before the ticket
+    }
     __syncthreads();
     if (threadIdx.x == 0)
         s_last = atomicAdd(&tickets[2 + blockIdx.x], 1u) == G - 1;
     __syncthreads();
-    if (s_last) {
+    if (!s_last)
+        return;
+    // the other CTAs' partials, read from L2
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (unsigned q = w; q < G; q += kMacWarps)
+        t = add4(t, __ldcg((const float4 *)&part[(size_t)q * pitch + b]));
+    red[w][lane] = t;
+    __syncthreads();
+    if (w == 0) {
+        float4 r = red[0][lane];
+#pragma unroll
+        for (int q = 1; q < kMacWarps; q++)
+            r = add4(r, red[q][lane]);
+        if (b < nb)
+            y[b] = make_float2(r.x * s, r.y * s);
+        if (b + 1 < nb)
+            y[b + 1] = make_float2(r.z * s, r.w * s);
+    }
+    if (threadIdx.x == 0) {
+        tickets[2 + blockIdx.x] = 0;
         __threadfence();
-        if (b < nb) {
-            float2 acc = make_float2(0.f, 0.f);
-            for (unsigned q = 0; q < G; q++) {
-                const float2 v = __ldcg(&part[(size_t)q * nb + b]);
-                acc.x += v.x;
-                acc.y += v.y;
-            }
-            y[b] = make_float2(acc.x * s, acc.y * s);
-        }
-        if (threadIdx.x == 0) {
-            tickets[2 + blockIdx.x] = 0;
+        if (atomicAdd(&tickets[1], 1u) == gridDim.x - 1) {
+            tickets[1] = 0;
+            tickets[0] = k + 1;
             __threadfence();
-            if (atomicAdd(&tickets[1], 1u) == gridDim.x - 1) {
-                tickets[1] = 0;
-                tickets[0] = k + 1;
-                __threadfence();
-            }
         }
     }
 }
@@ -191,17 +233,21 @@ cudaError_t launch_adjoint_filter_reduce(float2 *acc, const float2 *g, long long
     return cudaGetLastError();
 }
 
+unsigned upols_pitch(unsigned nb) { return (nb + kMacBins - 1) / kMacBins * kMacBins; }
+
+unsigned upols_groups(unsigned nb) { return (nb + kMacBins - 1) / kMacBins; }
+
 cudaError_t launch_upols_mac(float2 *y, const float2 *xcur, float2 *fdl, const float2 *h, float2 *part, unsigned nb,
                              unsigned P, unsigned G, unsigned *tickets, float s, cudaStream_t st)
 {
-    const unsigned gx = (nb + 255) / 256;
-    upols_mac<<<dim3(gx, G), 256, 0, st>>>(y, xcur, fdl, h, part, nb, P, tickets, s);
+    upols_mac<<<dim3(upols_groups(nb), G), kMacWarps * 32, 0, st>>>(y, xcur, fdl, h, part, nb, upols_pitch(nb), P,
+                                                                    tickets, s);
     return cudaGetLastError();
 }
 
 unsigned upols_chunks(unsigned nb, unsigned P, int sms)
 {
-    const unsigned gx = (nb + 255) / 256;
+    const unsigned gx = upols_groups(nb);
     const unsigned want = 4u * (unsigned)(sms > 0 ? sms : 152);
     unsigned G = (want + gx - 1) / gx;
     return G < 1 ? 1 : (G > P ? P : G);

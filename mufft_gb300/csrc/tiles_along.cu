@@ -32,6 +32,11 @@ void register_tiles_along(std::vector<TileKernel> &out)
     TILE_Q(16384, 16, 1, 4);
     TILE_Q(32768, 16, 1, 8);
     TILE_Q(65536, 16, 1, 8);
+    // narrower batched tiles (after the defaults above): finer grids for
+    // batches whose default grid fills the GPU about once
+    TILE(1024, 16, 1);
+    TILE(1024, 16, 2);
+    TILE(2048, 16, 1);
 }
 
 }  // namespace mgb

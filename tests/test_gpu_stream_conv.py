@@ -29,10 +29,25 @@ def linear_conv_f64(x, h):
     return np.fft.ifft(np.fft.fft(x.astype(np.complex128), L) * np.fft.fft(h.astype(np.float64), L))[: len(x)]
 
 
-def stream(gpu, block, method, h, x, restart_at=None):
+def stream(gpu, block, method, h, x, restart_at=None, fused=1, ranges=0):
     stereo = method & 1
-    conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, len(h), 0)
+    assert gpu.gb_set_stream_conv_fused(fused) == 0
+    assert gpu.gb_set_stream_conv_ranges(ranges) == 0
+    try:
+        conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, len(h), 0)
+    finally:
+        gpu.gb_set_stream_conv_fused(1)
+        gpu.gb_set_stream_conv_ranges(0)
     assert conv, gpu.gb_last_error_string()
+    # one fused launch per block exactly when a 256-thread row tile holds the window
+    M = 2 * block if stereo else block
+    assert gpu.gb_stream_conv_fused(conv) == (1 if fused and 64 <= M <= 4096 else 0)
+    P = (len(h) + block - 1) // block
+    if ranges:
+        most = max(1, P - 1) if gpu.gb_stream_conv_fused(conv) else P
+        used = gpu.gb_stream_conv_ranges(conv)
+        # fused launches keep every CTA resident: large requests are capped
+        assert used == min(ranges, most) if ranges <= 7 else 1 <= used <= min(ranges, most), (used, ranges, P)
     sample = 8 if stereo else 4
     out = np.zeros(len(x), np.complex64 if stereo else np.float32)
     try:
@@ -44,25 +59,45 @@ def stream(gpu, block, method, h, x, restart_at=None):
             assert gpu.gb_memcpy(inp, blk.ctypes.data, block * sample) == 0
             assert gpu.gb_stream_conv_process(conv, None) == 0, gpu.gb_last_error_string()
             assert gpu.gb_memcpy(out[k * block:].ctypes.data, outp, block * sample) == 0
+        assert gpu.gb_stream_conv_status(conv) == 0, gpu.gb_last_error_string()
     finally:
         gpu.gb_free_stream_conv(conv)
     return out
 
 
-@pytest.mark.parametrize("block", [64, 1024])
+@pytest.mark.parametrize("block", [8, 64, 1024])
 @pytest.mark.parametrize("taps_of", [lambda b: 1, lambda b: 100, lambda b: b, lambda b: 3 * b + 5, lambda b: 40 * b])
 @pytest.mark.parametrize("method", [0, STEREO])
-def test_stream_conv_matches_linear_convolution(gpu, block, taps_of, method):
+@pytest.mark.parametrize("fused", [1, 0])
+def test_stream_conv_matches_linear_convolution(gpu, block, taps_of, method, fused):
+    """One fused launch per block (forward row tile, multiply-accumulate and
+    inverse in one grid) and the graph of separate launches."""
     taps = taps_of(block)
     blocks = 12
     h = (signals.normal(60000 + taps, taps) * np.exp(-np.arange(taps) / max(1.0, taps / 4))).astype(np.float32)
     n = blocks * block
     x = signals.complex_uniform(61000 + block, n) if method & 1 else signals.uniform(61000 + block, n)
-    got = stream(gpu, block, method, h, x)
+    got = stream(gpu, block, method, h, x, fused=fused)
     ref = linear_conv_f64(x, h)
     if not method & 1:
         ref = ref.real
     assert rel_l2(got, ref) < 1e-5, (block, taps, method)
+
+
+@pytest.mark.parametrize("ranges", [1, 2, 7, 1000])
+@pytest.mark.parametrize("method", [0, STEREO])
+def test_stream_conv_partition_ranges(gpu, ranges, method):
+    """Any split of the partitions over CTA rows (tickets finish each bin
+    group in range order) gives the linear convolution."""
+    block, taps = 512, 512 * 37 + 3
+    h = (signals.normal(64000, taps) * np.exp(-np.arange(taps) / (taps / 4))).astype(np.float32)
+    x = signals.complex_uniform(64001, 10 * block) if method & 1 else signals.uniform(64001, 10 * block)
+    ref = linear_conv_f64(x, h)
+    if not method & 1:
+        ref = ref.real
+    for fused in (1, 0):
+        got = stream(gpu, block, method, h, x, fused=fused, ranges=ranges)
+        assert rel_l2(got, ref) < 1e-5, (ranges, method, fused)
 
 
 def test_stream_conv_long_filter(gpu):
