@@ -275,6 +275,10 @@ bool device_prepare(int *dev_out)
                                                   (int)k.smem),
                              "cudaFuncSetAttribute"))
                     return false;
+                if (k.fn_c2r && !cuda_ok(cudaFuncSetAttribute(k.fn_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                              (int)k.smem),
+                                         "cudaFuncSetAttribute"))
+                    return false;
             }
         }
         ds.ready = true;
@@ -478,7 +482,10 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                 cfg.numAttrs = 1;
                 e = cudaLaunchKernelExC(&cfg, p.k->fn, args);
             } else {
-                e = cudaLaunchKernel(p.k->fn, p.grid, dim3(p.k->threads), args, smem, st);
+                // c2r fix-up rows staged in shared memory where the tile has that variant
+                const bool c2r_rows = p.k->fn_c2r && (a.prologue == PRO_C2R || a.prologue == PRO_MUL_C2R) &&
+                                      a.mirror_ldist == 0 && a.mirror_len == p.k->L && !a.half && a.in_stride == 1;
+                e = cudaLaunchKernel(c2r_rows ? p.k->fn_c2r : p.k->fn, p.grid, dim3(p.k->threads), args, smem, st);
             }
             if (e != cudaSuccess)
                 return e;
@@ -781,8 +788,11 @@ bool attach_occupancy(std::vector<Pass> &ps, bool dry, int device)
         if (want <= p.k->smem)
             continue;
         p.smem_min = want;
-        if (!dry && !cuda_ok(cudaFuncSetAttribute(p.k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
-                             "cudaFuncSetAttribute(occupancy)"))
+        if (!dry && (!cuda_ok(cudaFuncSetAttribute(p.k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
+                              "cudaFuncSetAttribute(occupancy)") ||
+                     (p.k->fn_c2r && !cuda_ok(cudaFuncSetAttribute(p.k->fn_c2r,
+                                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
+                                              "cudaFuncSetAttribute(occupancy)"))))
             return false;
     }
     return true;
@@ -2638,6 +2648,10 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
         a.fwd.out = c->xcur;
         a.fwd.in2 = nullptr;
         a.inv = c->inv->passes[0].a;
+        a.inv_c2r_rows = (a.inv.prologue == PRO_C2R && a.inv.mirror_ldist == 0 && a.inv.mirror_len == (long long)M &&
+                          !a.inv.half && a.inv.in_stride == 1)
+                             ? 1
+                             : 0;
         a.inv.in = c->y;
         a.inv.out = (float2 *)c->ybuf;
         a.inv.in2 = nullptr;

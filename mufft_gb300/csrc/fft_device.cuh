@@ -434,6 +434,63 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
     }
 }
 
+// c2r fix-up prologue of a row tile (unit stride, mirror within the row):
+// element n of transform tr needs X[n] and X[M - n], which another thread
+// loads.  Conditions: prologue PRO_C2R or PRO_MUL_C2R, unit stride,
+// mirror_ldist 0, mirror_len L, no `half`.  The row is staged once, coalesced, in the transform's exchange
+// slice (padded positions), and both operands are read from there -- one
+// global load per element instead of two.  X[M] (needed by n = 0 only) is
+// loaded directly.  PRO_MUL_C2R multiplies by s * B[n] while staging.  Not
+// for zero-padded inputs (`half`).  The caller's CTA must not use the slice
+// until the next barrier.
+template <int L, int R, bool COH>
+__device__ __forceinline__ void load_stage0_c2r_rows(const TileArgs &a, const float2 *__restrict__ in,
+                                                     const float2 *__restrict__ in2, unsigned tr, int tl,
+                                                     float2 *region, float2 (&v)[R])
+{
+    using S = Sched<L, R>;
+    using TT = Tile<L, R, 1>;
+    constexpr int r = S::radix(0), NB = R / r, B = TT::B(0), TL = TT::TL;
+    const bool valid = tr < a.ntrans;
+    const bool mul = a.prologue == PRO_MUL_C2R;
+    const long long tbase = (long long)tr * a.in_dist;
+    auto fetch = [&](long long n) {
+        float2 xv = gload<COH>(in + tbase + n);
+        if (mul) {
+            float2 g = gload<COH>(in2 + tbase + n);
+            g.y = a.conj2 ? -g.y : g.y;
+            xv = cscale(cmul(xv, g), a.scale);
+        }
+        return xv;
+    };
+    if (valid) {
+#pragma unroll
+        for (int i = 0; i < R; i++)
+            region[padpos(tl + TL * i)] = fetch(tl + TL * i);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < R; q++)
+        v[q] = make_float2(0.f, 0.f);
+    if (valid) {
+#pragma unroll
+        for (int u = 0; u < NB; u++)
+#pragma unroll
+            for (int m = 0; m < r; m++) {
+                const int local = tl + TL * u + m * B;
+                const float2 xa = region[padpos(local)];
+                // only register 0 of thread 0 is position 0 (its mirror X[M] is not staged)
+                const float2 xb = (u == 0 && m == 0 && tl == 0) ? fetch(L) : region[padpos(L - local)];
+                v[u * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
+            }
+    }
+    if (a.conj & 1) {
+#pragma unroll
+        for (int q = 0; q < R; q++)
+            v[q].y = -v[q].y;
+    }
+}
+
 // Stage-0 inputs of a column tile already staged in shared memory (by TMA):
 // element n of the tile's column c at sin[n*C + c].  Plain prologue only.
 template <int L, int R, int C>
@@ -562,7 +619,10 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // base (batches); j is the CTA's rank in its cluster.  COH: load with
 // L2-coherent loads (input written earlier in the same launch).
 // PRE: the stage-0 registers were loaded by the caller (`pre`, R values).
-template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false, bool PRE = false>
+// C2RS: c2r fix-up prologue through a row staged in shared memory (row
+// tiles; the caller checked load_stage0_c2r_rows's conditions).
+template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false, bool PRE = false,
+          bool C2RS = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
                                           float2 *smem, const float2 *sin = nullptr, unsigned twy = 0,
                                           const float2 *pre = nullptr)
@@ -619,6 +679,10 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     } else if constexpr (SIN) {
         static_assert(Q == 1 && LMAP == ACROSS, "staged inputs are column tiles");
         load_stage0_sin<L, R, C>(a, sin, tile0 + c, c, tl, v);
+    } else if constexpr (C2RS) {
+        static_assert(LMAP == ALONG && Q == 1 && NST > 1, "staged c2r rows need a row tile with an exchange");
+        load_stage0_c2r_rows<L, R, COH>(a, in, in2, tile0 + c, tl, smem + c * RS, v);
+        __syncthreads();  // the exchange slices are free again
     } else {
         load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
     }
@@ -769,6 +833,34 @@ __global__ void __launch_bounds__(tile_threads<L, R, C, Q>(), tile_min_blocks<L,
         tile = blockIdx.x / Q;
     }
     tile_body<L, R, C, Q, LMAP, SMAP, false>(a, tile, j, ioff, ooff, smem, nullptr, blockIdx.y);
+}
+
+// Row tile whose c2r fix-up prologue stages each row in shared memory
+// (load_stage0_c2r_rows); one CTA per tile as tile_fft.
+template <int L, int R, int C>
+__global__ void __launch_bounds__(tile_threads<L, R, C, 1>(), tile_min_blocks<L, R, C, 1>())
+    tile_fft_c2r_rows(const TileArgs a)
+{
+    extern __shared__ float2 smem[];
+    long long ioff, ooff;
+    if (a.ysplit) {
+        const unsigned g = blockIdx.y % a.ysplit, b = blockIdx.y / a.ysplit;
+        ioff = (long long)g * a.in_batch + (long long)b * a.in_batch2;
+        ooff = (long long)g * a.out_batch + (long long)b * a.out_batch2;
+    } else {
+        ioff = (long long)blockIdx.y * a.in_batch;
+        ooff = (long long)blockIdx.y * a.out_batch;
+    }
+    tile_body<L, R, C, 1, ALONG, ALONG, false, false, false, true>(a, blockIdx.x, 0, ioff, ooff, smem);
+}
+
+// The staged-c2r variant of a row tile, or null where there is none.
+template <int L, int R, int C, int Q> constexpr const void *tile_c2r_rows_fn()
+{
+    if constexpr (Q == 1 && Sched<L, R>::NST > 1)
+        return (const void *)&tile_fft_c2r_rows<L, R, C>;
+    else
+        return nullptr;
 }
 
 }  // namespace mgb

@@ -18,6 +18,7 @@ struct TileKernel {
     size_t smem;    // per CTA
     bool has_thi;   // column pass that takes the four-step twiddle table tw_lo
     size_t smem_ex; // per CTA without the four-step table region (launches with tw_lo == null)
+    const void *fn_c2r = nullptr;  // row tiles: variant staging c2r fix-up rows in shared memory
 };
 
 void register_tiles_along(std::vector<TileKernel> &out);

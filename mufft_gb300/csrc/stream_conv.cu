@@ -176,7 +176,10 @@ __global__ void __launch_bounds__(256) upols_block(const UpolsBlockArgs a)
     __syncthreads();
     if (flag) {
         // every group is finished: y is complete (L2-coherent loads)
-        tile_body<M, 16, C, 1, ALONG, ALONG, true>(a.inv, 0, 0, 0, 0, smem);
+        if (a.inv_c2r_rows)
+            tile_body<M, 16, C, 1, ALONG, ALONG, true, false, false, true>(a.inv, 0, 0, 0, 0, smem);
+        else
+            tile_body<M, 16, C, 1, ALONG, ALONG, true>(a.inv, 0, 0, 0, 0, smem);
         if (threadIdx.x == 0) {
             a.tickets[1] = 0;  // read again by the next launch only
             a.tickets[0] = k + 1;

@@ -10,6 +10,7 @@ namespace mgb {
 struct UpolsBlockArgs {
     TileArgs fwd;        // forward transform: window -> xcur (256-thread row tile, one transform)
     TileArgs inv;        // inverse transform: y -> output window
+    int inv_c2r_rows;    // the inverse's c2r fix-up stages y in shared memory (load_stage0_c2r_rows)
     float2 *xcur;        // nb bins: spectrum of the current window
     float2 *fdl;         // P rows of `pitch` bins: spectra of the last P windows (block j in slot j % P)
     const float2 *h;     // P rows of `pitch` bins: filter-partition spectra (pad bins zero)

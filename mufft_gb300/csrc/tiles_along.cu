@@ -7,7 +7,8 @@ namespace mgb {
 #define TILE_Q(L, R, C, Q)                                                                            \
     out.push_back(TileKernel{L, R, C, Q, ALONG, ALONG, (const void *)&tile_fft<L, R, C, Q, ALONG, ALONG>, \
                              C *(L / (R * Q)), tile_smem_bytes<L, R, C, Q, ALONG, ALONG>(),                \
-                             tile_has_thi<L, R, C, Q, ALONG, ALONG>(), tile_exchange_bytes<L, R, C, Q, ALONG, ALONG>()})
+                             tile_has_thi<L, R, C, Q, ALONG, ALONG>(), tile_exchange_bytes<L, R, C, Q, ALONG, ALONG>(), \
+                             tile_c2r_rows_fn<L, R, C, Q>()})
 #define TILE(L, R, C) TILE_Q(L, R, C, 1)
 
 void register_tiles_along(std::vector<TileKernel> &out)
