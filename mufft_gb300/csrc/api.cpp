@@ -2123,7 +2123,7 @@ bool enqueue_class(mufft_gb_conv_batch *b, unsigned lg, bool stereo, bool zp, co
                    cudaStream_t st)
 {
     const int L1 = lg == 16 ? 256 : 128, L2 = lg == 14 ? 128 : 256, L = L1 * L2;
-    const ClassTile ct = class_column_tile(L1), rt = class_row_tile(L2);
+    const ClassTile ct = class_column_tile(L1), rt = class_row_tile(L2), rmt = class_row_mul_tile(L2);
     TileArgs base{};
     base.tw = g_dev[b->device].tw;
     base.scale = 1.0f;
@@ -2143,8 +2143,16 @@ bool enqueue_class(mufft_gb_conv_batch *b, unsigned lg, bool stereo, bool zp, co
     ph[3].conj = 1;
     ph[3].epilogue = EPI_TWIDDLE;
     ph[4].conj = 2;
+    if (stereo) {
+        // the spectral multiply rides in F2's epilogue: X[k1 + L1*k2] * H[k1 + L1*k2] / L
+        ph[1].in2_dist = 1;
+        ph[1].in2_stride = L1;
+        ph[1].scale = 1.0f / (float)L;
+    }
     for (int phase = 0; phase < 5; phase++) {
         cudaError_t e;
+        if (phase == 2 && stereo)
+            continue;
         if (phase == 2) {
             const unsigned l1 = ilog2u((unsigned)L1), l2 = ilog2u((unsigned)L2);
             int st_ = stereo ? 1 : 0;
@@ -2153,7 +2161,7 @@ bool enqueue_class(mufft_gb_conv_batch *b, unsigned lg, bool stereo, bool zp, co
             void *args[] = {(void *)&tab, (void *)&l1, (void *)&l2, &st_, &scale, (void *)&rf, (void *)&ri};
             e = cudaLaunchKernel(class_multiply_fn(), dim3((unsigned)(L / 2048), K), dim3(256), args, 0, st);
         } else {
-            const ClassTile &t = (phase == 0 || phase == 4) ? ct : rt;
+            const ClassTile &t = (phase == 0 || phase == 4) ? ct : (phase == 1 && stereo ? rmt : rt);
             const unsigned tiles = (phase == 0 || phase == 4) ? (unsigned)(L2 / t.C) : (unsigned)(L1 / t.C);
             int phase_ = phase;
             void *args[] = {&ph[phase], (void *)&tab, &phase_};

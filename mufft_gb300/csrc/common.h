@@ -76,6 +76,9 @@ struct TileArgs {
     long long mirror_ldist;   // see tile kernel: local index = t*ldist + n*stride
     // convolution prologues
     const float2 *in2;        // second spectrum (B)
+    // multiply epilogue (class pipelines): output k of transform t times
+    // scale * in2[t*in2_dist + k*in2_stride]
+    long long in2_dist, in2_stride;
     float scale;
     int conj2;                // multiply by conj(B) instead (adjoint of the convolution)
     // four-step twiddle W_N^m = exp(-2*pi*i*m/N): tw_scale = 2/N, tw_mask = N - 1;

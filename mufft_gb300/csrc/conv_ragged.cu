@@ -334,6 +334,24 @@ __global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L
     tile_body<L, 16, C, 1, LMAP, SMAP, false>(a, blockIdx.x, 0, 0, 0, smem);
 }
 
+// Phase 1 of a stereo class with the spectral multiply fused into its
+// epilogue: rows k1 of X^T[k1][k2] = X[k1 + L1*k2], times s * H[k1 + L1*k2]
+// (the template's in2_dist = 1, in2_stride = L1); the multiply launch is
+// skipped.  Neighbouring rows of a tile read H's neighbouring elements.
+template <int L, int C>
+__global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L, 16, C, 1>())
+    class_tile_mul(const TileArgs tmpl, const ClassEntry *tab, int phase)
+{
+    extern __shared__ float2 smem[];
+    const ClassEntry e = tab[blockIdx.y];
+    TileArgs a = tmpl;
+    a.in = e.spec;
+    a.out = e.spec;
+    a.in2 = e.h;
+    (void)phase;
+    tile_body<L, 16, C, 1, ALONG, ALONG, false, false, false, false, true>(a, blockIdx.x, 0, 0, 0, smem);
+}
+
 // The multiply phase for a table of requests (blockIdx.y), on the transposed
 // spectrum X^T[k1][k2] = X[k1 + L1*k2] of L = L1 x L2 points, as
 // conv_multiply above.
@@ -391,6 +409,15 @@ ClassTile class_row_tile(int L2)
         return ClassTile{(const void *)&class_tile<128, 32, ALONG, ALONG>, 128, 32, tile_threads<128, 16, 32, 1>(),
                          tile_smem_bytes<128, 16, 32, 1, ALONG, ALONG>()};
     return ClassTile{(const void *)&class_tile<256, 16, ALONG, ALONG>, 256, 16, tile_threads<256, 16, 16, 1>(),
+                     tile_smem_bytes<256, 16, 16, 1, ALONG, ALONG>()};
+}
+
+ClassTile class_row_mul_tile(int L2)
+{
+    if (L2 == 128)
+        return ClassTile{(const void *)&class_tile_mul<128, 32>, 128, 32, tile_threads<128, 16, 32, 1>(),
+                         tile_smem_bytes<128, 16, 32, 1, ALONG, ALONG>()};
+    return ClassTile{(const void *)&class_tile_mul<256, 16>, 256, 16, tile_threads<256, 16, 16, 1>(),
                      tile_smem_bytes<256, 16, 16, 1, ALONG, ALONG>()};
 }
 

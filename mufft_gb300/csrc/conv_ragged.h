@@ -69,6 +69,10 @@ struct ClassTile {
 // Phase 0/4 (columns of L1) and 1/3 (rows of L2) tiles for a split L1 x L2.
 ClassTile class_column_tile(int L1);
 ClassTile class_row_tile(int L2);
+// Phase 1 with the stereo spectral multiply fused, kernel(TileArgs tmpl,
+// const ClassEntry *tab, int phase) with the template's in2_dist = 1,
+// in2_stride = L1 and scale = 1 / L; the multiply launch is then skipped.
+ClassTile class_row_mul_tile(int L2);
 const void *class_multiply_fn();  // kernel(const ClassEntry *tab, unsigned l1, unsigned l2, int stereo, float scale,
                                   //        const float2 *rtw_fwd, const float2 *rtw_inv)
 

@@ -621,8 +621,10 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // PRE: the stage-0 registers were loaded by the caller (`pre`, R values).
 // C2RS: c2r fix-up prologue through a row staged in shared memory (row
 // tiles; the caller checked load_stage0_c2r_rows's conditions).
+// EMUL: plain epilogue multiplied by scale * in2[tr*in2_dist + k*in2_stride]
+// (the spectral multiply of a convolution, fused into the forward pass).
 template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false, bool PRE = false,
-          bool C2RS = false>
+          bool C2RS = false, bool EMUL = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
                                           float2 *smem, const float2 *sin = nullptr, unsigned twy = 0,
                                           const float2 *pre = nullptr)
@@ -804,7 +806,10 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
 #pragma unroll
                 for (int m = 0; m < rl; m++) {
                     const int off = TL * u + m * Q * BL;
-                    const float2 y = v[u * rl + m];
+                    float2 y = v[u * rl + m];
+                    if constexpr (EMUL)
+                        y = cscale(cmul(y, __ldg(&a.in2[(long long)tr * a.in2_dist + (long long)(p0 + off) * a.in2_stride])),
+                                   a.scale);
                     o0[(long long)off * sst] = make_float2(y.x, sg * y.y);
                 }
         }
