@@ -680,15 +680,24 @@ def companion_adjoint(lib, torch) -> dict:
 
     def gd_step():
         assert lib.gb_execute_conv_input_async(plan, K.CONV_BLOCK_SECOND, H.data_ptr(), h.data_ptr(), sp) == 0
+        assert lib.gb_execute_conv_output_batched(plan, y.data_ptr(), N, A.data_ptr(), nblk, H.data_ptr(), B, sp) == 0
+        y.sub_(ystar)  # residual r = conv(x, h) - y*
+        assert lib.gb_conv_adjoint(plan, gh.data_ptr(), gx.data_ptr(), N, y.data_ptr(), N, A.data_ptr(), nblk,
+                                   H.data_ptr(), B, sp) == 0
+        h[:T].sub_(lr * gh[:T])
+
+    def gd_step_per_signal():  # the same step through the one-signal entry points
+        assert lib.gb_execute_conv_input_async(plan, K.CONV_BLOCK_SECOND, H.data_ptr(), h.data_ptr(), sp) == 0
         for b in range(B):
             lib.gb_execute_conv_output_async(plan, y[b].data_ptr(), A[b].data_ptr(), H.data_ptr(), sp)
-        y.sub_(ystar)  # residual r = conv(x, h) - y*
+        y.sub_(ystar)
         assert lib.gb_conv_adjoint_filter(plan, gh.data_ptr(), y.data_ptr(), N, A.data_ptr(), nblk, B, sp) == 0
         for b in range(B):
             lib.gb_conv_adjoint_input(plan, gx[b].data_ptr(), y[b].data_ptr(), H.data_ptr(), sp)
         h[:T].sub_(lr * gh[:T])
 
     ms = _time_ms(torch, gd_step, reps=5)
+    ms_per_signal = _time_ms(torch, gd_step_per_signal, reps=3)
     # accuracy: both gradients for two of the signals against FP64 (numpy)
     y2 = torch.empty((2, N), dtype=torch.complex64, device="cuda")
     gh2 = torch.empty(N, device="cuda")
@@ -714,13 +723,16 @@ def companion_adjoint(lib, torch) -> dict:
            "grad_input_rel_l2_vs_fp64": float(np.linalg.norm(gx0.cpu().numpy() - gx_ref) / np.linalg.norm(gx_ref)),
            "checked": "2 of the 64 signals, FP64 numpy gradients of the same residual"}
     lib.free_plan_conv(plan)
-    fft_flops = 5.0 * N * math.log2(N) * (2 * B + 2 * B + 2)  # conv_output, adjoint input, gradient spectra, filter
+    # transforms per step: B conv outputs, B output-gradient spectra (shared by
+    # both adjoints), B input-gradient inverses, the filter spectrum and its c2r
+    fft_flops = 5.0 * N * math.log2(N) * (3 * B + 2)
     del x, A, ystar, y, gx
     torch.cuda.empty_cache()
     return {"workload": "64 stereo signals x 2^20 frames, 2^16-tap filter, N = 2^21, loss 0.5||conv(x,h) - y*||^2",
             "step_ms": ms,
-            "step": "filter spectrum + 64 conv_output + residual + filter adjoint (64 signals) + 64 input adjoints "
-                    "+ update; first-block spectra cached",
+            "step": "filter spectrum + batched conv output (64 signals) + residual + both adjoints in one call "
+                    "(one forward transform per output gradient) + update; first-block spectra cached",
+            "per_signal_step_ms": ms_per_signal,
             "fft_GFLOP/s": fft_flops / (ms * 1e-3) / 1e9, "accuracy": acc}
 
 

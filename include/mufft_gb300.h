@@ -120,6 +120,23 @@ int mufft_gb_conv_adjoint_filter(mufft_plan_conv *plan, float *grad_filter, cons
                                  size_t output_dist, const void *first_spectra, size_t spectrum_dist,
                                  unsigned batch, void *stream);
 
+/* Both gradients of `batch` signals sharing one second block, each output
+ * gradient transformed once for both (batched launches over chunks of
+ * signals): grad_filter as mufft_gb_conv_adjoint_filter (NULL: not computed)
+ * and grad_inputs, batch blocks `input_dist` samples apart, each as
+ * mufft_gb_conv_adjoint_input (NULL: not computed).  Device buffers. */
+int mufft_gb_conv_adjoint(mufft_plan_conv *plan, float *grad_filter, void *grad_inputs, size_t input_dist,
+                          const void *grad_outputs, size_t output_dist, const void *first_spectra,
+                          size_t spectrum_dist, const void *second_spectrum, unsigned batch, void *stream);
+
+/* mufft_execute_conv_output for `batch` signals sharing one second block:
+ * outputs `output_dist` samples apart, first spectra `spectrum_dist` complex
+ * apart, one filter spectrum for all (batched launches over chunks of
+ * signals).  Device buffers. */
+int mufft_gb_execute_conv_output_batched(mufft_plan_conv *plan, void *outputs, size_t output_dist,
+                                         const void *first_spectra, size_t spectrum_dist, const void *second_spectrum,
+                                         unsigned batch, void *stream);
+
 /* --------------------------------------------- ragged batched convolution */
 
 /* No counterpart in the reference, which convolves one block per call

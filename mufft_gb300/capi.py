@@ -91,6 +91,8 @@ GB_H = [
     ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
     ("conv_adjoint_input", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
+    ("conv_adjoint", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _u, _vp]),
+    ("execute_conv_output_batched", _i, [_vp, _vp, _sz, _vp, _sz, _vp, _u, _vp]),
     ("set_split_engine", _i, [_i]),
     ("set_tma", _i, [_i]),
     ("set_tile_occupancy", _i, [_i]),

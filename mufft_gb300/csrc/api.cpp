@@ -1760,6 +1760,14 @@ struct mufft_plan_conv {
     float2 *adj_spec = nullptr;              // spectra of the gradients
     size_t adj_spec_bytes = 0;
     float2 *adj_acc = nullptr;               // N/2 + 1 bins of the filter gradient
+    // batched forms (mufft_gb_execute_conv_output_batched, mufft_gb_conv_adjoint):
+    // plans over a chunk of signals and over the ragged last chunk
+    struct BatchPlan {
+        mufft_plan_1d *pl = nullptr;
+        unsigned batch = 0;
+        size_t idist = 0, odist = 0;
+    };
+    BatchPlan out_b[2], fwd_b[2], inv_b[2];
 };
 
 extern "C" {
@@ -1843,6 +1851,11 @@ void mufft_free_plan_conv(mufft_plan_conv *plan)
 {
     if (!plan)
         return;
+    for (int i = 0; i < 2; i++) {
+        destroy_1d(plan->out_b[i].pl);
+        destroy_1d(plan->fwd_b[i].pl);
+        destroy_1d(plan->inv_b[i].pl);
+    }
     destroy_1d(plan->in_plan[0]);
     destroy_1d(plan->in_plan[1]);
     destroy_1d(plan->out_plan);
@@ -1991,6 +2004,156 @@ int mufft_gb_conv_adjoint_filter(mufft_plan_conv *plan, float *grad_filter, cons
             return t_err;
     }
     return exec_1d(plan->adj_c2r, grad_filter, plan->adj_acc, nullptr, st, false);
+}
+
+}  // extern "C"
+
+namespace {
+
+// A batched plan of `batch` transforms, remade when its shape changes.  With
+// a prologue (spectral multiply) the second spectrum is one for the whole
+// batch (in2_bcast).
+mufft_plan_1d *conv_batch_plan(mufft_plan_conv::BatchPlan &bp, int kind, unsigned N, int direction, unsigned batch,
+                               size_t idist, size_t odist, int prologue, bool conj2)
+{
+    if (bp.pl && bp.batch == batch && bp.idist == idist && bp.odist == odist)
+        return bp.pl;
+    destroy_1d(bp.pl);
+    bp = mufft_plan_conv::BatchPlan{};
+    mufft_plan_1d *pl = create_1d(kind, N, direction, 0, batch, idist, odist, prologue, false, nullptr, conj2);
+    if (!pl)
+        return nullptr;
+    for (Pass &p : pl->passes)
+        if (p.type == PASS_TILE && p.in2_role != ROLE_NONE)
+            p.a.in2_bcast = pl->passes.size() == 1 ? 2 : 1;  // batch by transform index / by grid row
+    bp.pl = pl;
+    bp.batch = batch;
+    bp.idist = idist;
+    bp.odist = odist;
+    return pl;
+}
+
+// Signals per chunk of a batched convolution call: spectra (and multi-pass
+// scratch) of a chunk stay within 256 MiB.
+size_t conv_chunk(const mufft_plan_conv *c, unsigned batch)
+{
+    size_t chunk = ((size_t)256 << 20) / (conv_bins(c) * sizeof(float2));
+    chunk = chunk < 1 ? 1 : chunk;
+    return chunk > batch ? batch : chunk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mufft_gb_execute_conv_output_batched(mufft_plan_conv *plan, void *outputs, size_t output_dist,
+                                         const void *first_spectra, size_t spectrum_dist, const void *second_spectrum,
+                                         unsigned batch, void *stream)
+{
+    if (!plan || !outputs || !first_spectra || !second_spectrum || batch == 0) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer, or empty batch");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    t_err = 0;
+    const bool stereo = conv_stereo(plan);
+    const unsigned N = plan->N;
+    if (output_dist < N || (!stereo && (output_dist & 1)) || spectrum_dist < conv_bins(plan)) {
+        set_error(MUFFT_GB_ERR_INVALID, "batch distances smaller than one block");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (!is_device_accessible(outputs) || !is_device_accessible(first_spectra) ||
+        !is_device_accessible(second_spectrum)) {
+        set_error(MUFFT_GB_ERR_HOST_POINTER, "batched convolution needs device-accessible buffers");
+        return MUFFT_GB_ERR_HOST_POINTER;
+    }
+    DeviceGuard g(plan->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    const size_t chunk = conv_chunk(plan, batch);
+    const size_t elem = stereo ? sizeof(float2) : sizeof(float);
+    for (size_t b0 = 0; b0 < batch; b0 += chunk) {
+        const size_t n = batch - b0 < chunk ? batch - b0 : chunk;
+        mufft_plan_1d *pl = conv_batch_plan(plan->out_b[n == chunk ? 0 : 1], stereo ? K_C2C : K_C2R, N,
+                                            MUFFT_INVERSE, (unsigned)n, spectrum_dist, output_dist,
+                                            stereo ? PRO_MUL : PRO_MUL_C2R, false);
+        if (!pl)
+            return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+        const int rc = exec_1d(pl, (char *)outputs + b0 * output_dist * elem,
+                               (const float2 *)first_spectra + b0 * spectrum_dist, second_spectrum, st, false);
+        if (rc != MUFFT_GB_OK)
+            return rc;
+    }
+    return MUFFT_GB_OK;
+}
+
+int mufft_gb_conv_adjoint(mufft_plan_conv *plan, float *grad_filter, void *grad_inputs, size_t input_dist,
+                          const void *grad_outputs, size_t output_dist, const void *first_spectra,
+                          size_t spectrum_dist, const void *second_spectrum, unsigned batch, void *stream)
+{
+    if (!plan || !grad_outputs || batch == 0 || (!grad_filter && !grad_inputs) || (grad_filter && !first_spectra) ||
+        (grad_inputs && !second_spectrum)) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer, nothing to compute, or empty batch");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    t_err = 0;
+    const bool stereo = conv_stereo(plan);
+    const unsigned N = plan->N;
+    const size_t bins = conv_bins(plan);
+    if (output_dist < N || (!stereo && (output_dist & 1)) || (grad_filter && spectrum_dist < bins) ||
+        (grad_inputs && (input_dist < N || (!stereo && (input_dist & 1))))) {
+        set_error(MUFFT_GB_ERR_INVALID, "batch distances smaller than one block");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (!is_device_accessible(grad_outputs) || (grad_filter && (!is_device_accessible(grad_filter) ||
+                                                                !is_device_accessible(first_spectra))) ||
+        (grad_inputs && (!is_device_accessible(grad_inputs) || !is_device_accessible(second_spectrum)))) {
+        set_error(MUFFT_GB_ERR_HOST_POINTER, "the adjoint needs device-accessible buffers");
+        return MUFFT_GB_ERR_HOST_POINTER;
+    }
+    DeviceGuard g(plan->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    const size_t chunk = conv_chunk(plan, batch);
+    const size_t elem = stereo ? sizeof(float2) : sizeof(float);
+    if (!conv_adj_spec(plan, chunk * bins * sizeof(float2)))
+        return t_err;
+    if (grad_filter) {
+        if (!plan->adj_c2r)
+            plan->adj_c2r = create_1d(K_C2R, N, MUFFT_INVERSE, 0, 1, 0, 0, -1, false, nullptr);
+        if (!plan->adj_c2r)
+            return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+        if (!plan->adj_acc && !cuda_ok(cudaMalloc(&plan->adj_acc, (N / 2 + 1) * sizeof(float2)), "cudaMalloc"))
+            return t_err;
+    }
+    const float2 *A = (const float2 *)first_spectra;
+    for (size_t b0 = 0; b0 < batch; b0 += chunk) {
+        const size_t n = batch - b0 < chunk ? batch - b0 : chunk;
+        const int w = n == chunk ? 0 : 1;
+        // one forward transform of each output gradient serves both gradients
+        mufft_plan_1d *fwd = conv_batch_plan(plan->fwd_b[w], stereo ? K_C2C : K_R2C, N, MUFFT_FORWARD, (unsigned)n,
+                                             output_dist, bins, -1, false);
+        if (!fwd)
+            return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+        int rc = exec_1d(fwd, plan->adj_spec, (const char *)grad_outputs + b0 * output_dist * elem, nullptr, st, false);
+        if (rc != MUFFT_GB_OK)
+            return rc;
+        if (grad_filter &&
+            !cuda_ok(launch_adjoint_filter_reduce(plan->adj_acc, plan->adj_spec, (long long)bins,
+                                                  A + b0 * spectrum_dist, (long long)spectrum_dist, (unsigned)n, N,
+                                                  stereo ? 1 : 0, 1.0f / (float)N, b0 > 0 ? 1 : 0, st),
+                     "adjoint reduce"))
+            return t_err;
+        if (grad_inputs) {
+            mufft_plan_1d *inv = conv_batch_plan(plan->inv_b[w], stereo ? K_C2C : K_C2R, N, MUFFT_INVERSE,
+                                                 (unsigned)n, bins, input_dist, stereo ? PRO_MUL : PRO_MUL_C2R, true);
+            if (!inv)
+                return t_err ? t_err : MUFFT_GB_ERR_ALLOC;
+            rc = exec_1d(inv, (char *)grad_inputs + b0 * input_dist * elem, plan->adj_spec, second_spectrum, st, false);
+            if (rc != MUFFT_GB_OK)
+                return rc;
+        }
+    }
+    if (grad_filter)
+        return exec_1d(plan->adj_c2r, grad_filter, plan->adj_acc, nullptr, st, false);
+    return MUFFT_GB_OK;
 }
 
 }  // extern "C"

@@ -79,6 +79,10 @@ struct TileArgs {
     // multiply epilogue (class pipelines): output k of transform t times
     // scale * in2[t*in2_dist + k*in2_stride]
     long long in2_dist, in2_stride;
+    // one in2 for the whole batch (a filter spectrum shared by many signals):
+    // bit 0 -- not offset by the grid row's batch (multi-pass passes), bit 1 --
+    // not offset by the transform index (single-pass batched tiles)
+    int in2_bcast;
     float scale;
     int conj2;                // multiply by conj(B) instead (adjoint of the convolution)
     // four-step twiddle W_N^m = exp(-2*pi*i*m/N): tw_scale = 2/N, tw_mask = N - 1;

@@ -387,7 +387,7 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
         break;
     }
     case PRO_MUL: {
-        const float2 *g = in2 + tbase + p0 * sst;
+        const float2 *g = in2 + ((a.in2_bcast & 2) ? 0 : tbase) + p0 * sst;
 #pragma unroll
         for (int u = 0; u < NB; u++)
 #pragma unroll
@@ -414,7 +414,8 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
                     const long long ia = tb + local, ib = tb + a.mirror_len - local;
                     float2 xa = gload<COH>(&in[ia]), xb = gload<COH>(&in[ib]);
                     if (mul) {
-                        float2 ga = gload<COH>(&in2[ia]), gb = gload<COH>(&in2[ib]);
+                        const long long i2 = (a.in2_bcast & 2) ? tb : 0;  // (single-pass: tb is the transform's base)
+                        float2 ga = gload<COH>(&in2[ia - i2]), gb = gload<COH>(&in2[ib - i2]);
                         if (a.conj2) {
                             ga.y = -ga.y;
                             gb.y = -gb.y;
@@ -457,7 +458,7 @@ __device__ __forceinline__ void load_stage0_c2r_rows(const TileArgs &a, const fl
     auto fetch = [&](long long n) {
         float2 xv = gload<COH>(in + tbase + n);
         if (mul) {
-            float2 g = gload<COH>(in2 + tbase + n);
+            float2 g = gload<COH>(in2 + ((a.in2_bcast & 2) ? 0 : tbase) + n);
             g.y = a.conj2 ? -g.y : g.y;
             xv = cscale(cmul(xv, g), a.scale);
         }
@@ -637,7 +638,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     static_assert(NST > 1 || Q == 1, "single-stage tiles are not split over a cluster");
 
     const float2 *in = a.in + ioff;
-    const float2 *in2 = a.in2 ? a.in2 + ioff : nullptr;
+    const float2 *in2 = a.in2 ? a.in2 + ((a.in2_bcast & 1) ? 0 : ioff) : nullptr;
     float2 *out = a.out + ooff;
     const unsigned tile0 = tile * C;
 

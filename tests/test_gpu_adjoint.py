@@ -194,3 +194,74 @@ def test_gradient_descent_recovers_filter(gpu, torch):
     far = [i for i in range(1, len(losses)) if losses[i - 1] > 1e-6 * losses[0]]
     assert len(far) >= 5 and all(losses[i] <= losses[i - 1] for i in far), losses[:12]
     assert rel_l2(h_got, h_true) < 1e-4
+
+
+@pytest.mark.parametrize("N,B", [(256, 5), (4096, 3), (1 << 17, 3), (1 << 23, 5)])
+@pytest.mark.parametrize("method", [0, STEREO, PAD1 | PAD2, STEREO | PAD1])
+def test_batched_conv_output_and_adjoint_vs_fp64(gpu, torch, N, B, method):
+    """mufft_gb_execute_conv_output_batched and mufft_gb_conv_adjoint (one
+    filter spectrum broadcast over the batch; one forward transform of each
+    output gradient for both gradients) against FP64.  Single-pass (N <=
+    16384: the filter is shared across transforms of one tile) and
+    multi-pass sizes; (2^23, 5) runs a ragged last chunk (stereo)."""
+    if N == 1 << 23 and not method & 1:
+        pytest.skip("the ragged chunk needs the stereo spectrum size")
+    pl = ConvPlan(gpu, N, method)
+    try:
+        stereo = pl.stereo
+        firsts = np.stack([_signal(33000 + N + i, N, stereo) for i in range(B)])
+        grads = np.stack([_signal(34000 + N + i, N, stereo) for i in range(B)])
+        b = signals.uniform(35000 + N, N)
+        H = pl.spectrum(torch, K.CONV_BLOCK_SECOND, _dev(torch, b))
+        dA = torch.empty((B, pl.block), dtype=torch.complex64, device="cuda")
+        for i in range(B):
+            dA[i] = pl.spectrum(torch, K.CONV_BLOCK_FIRST, _dev(torch, firsts[i]))
+        dt = torch.complex64 if stereo else torch.float32
+        outs = torch.full((B, N), float("nan"), dtype=dt, device="cuda")
+        rc = gpu.gb_execute_conv_output_batched(pl.p, outs.data_ptr(), N, dA.data_ptr(), pl.block, H.data_ptr(), B,
+                                                _st(torch))
+        assert rc == 0, gpu.gb_last_error_string()
+        dg = _dev(torch, grads)
+        gx = torch.full((B, N), float("nan"), dtype=dt, device="cuda")
+        gh = torch.full((N,), float("nan"), dtype=torch.float32, device="cuda")
+        rc = gpu.gb_conv_adjoint(pl.p, gh.data_ptr(), gx.data_ptr(), N, dg.data_ptr(), N, dA.data_ptr(), pl.block,
+                                 H.data_ptr(), B, _st(torch))
+        assert rc == 0, gpu.gb_last_error_string()
+        # one gradient at a time gives the same numbers as both at once
+        gx2 = torch.full((B, N), float("nan"), dtype=dt, device="cuda")
+        rc = gpu.gb_conv_adjoint(pl.p, None, gx2.data_ptr(), N, dg.data_ptr(), N, None, 0, H.data_ptr(), B,
+                                 _st(torch))
+        assert rc == 0, gpu.gb_last_error_string()
+        torch.cuda.synchronize()
+    finally:
+        pl.free()
+    f_eff = firsts.astype(np.complex128 if stereo else np.float64)
+    if method & PAD1:
+        f_eff[:, N // 2:] = 0
+    b_eff = b.astype(np.float64)
+    if method & PAD2:
+        b_eff[N // 2:] = 0
+    got_out, got_gx = outs.cpu().numpy(), gx.cpu().numpy()
+    for i in range(B):
+        assert rel_l2(got_out[i], A.conv_f64(f_eff[i], b_eff, stereo)) < ADJ_TOL, i
+        assert rel_l2(got_gx[i], A.adjoint_input_f64(grads[i], b_eff, stereo)) < ADJ_TOL, i
+    assert rel_l2(gh.cpu().numpy(), A.adjoint_filter_f64(grads, f_eff)) < ADJ_TOL
+    assert np.array_equal(got_gx.view(np.uint32), gx2.cpu().numpy().view(np.uint32))
+
+
+def test_batched_adjoint_rejects_bad_arguments(gpu, torch):
+    pl = ConvPlan(gpu, 1024, STEREO)
+    try:
+        d = torch.zeros(4 * 1024, dtype=torch.complex64, device="cuda")
+        p = d.data_ptr()
+        # nothing to compute; distances below one block; empty batch
+        for args in [(None, None, 1024, p, 1024, p, pl.block, p, 2),
+                     (p, p, 512, p, 1024, p, pl.block, p, 2),
+                     (p, p, 1024, p, 1024, p, 16, p, 2),
+                     (p, p, 1024, p, 1024, p, pl.block, p, 0)]:
+            assert gpu.gb_conv_adjoint(pl.p, *args, _st(torch)) != 0
+            gpu.gb_clear_error()
+        assert gpu.gb_execute_conv_output_batched(pl.p, p, 512, p, pl.block, p, 2, _st(torch)) != 0
+        gpu.gb_clear_error()
+    finally:
+        pl.free()
