@@ -2229,6 +2229,7 @@ struct mufft_gb_conv_batch {
     RaggedArgs args{};
     size_t smem = 0;
     ClassEntry *d_class = nullptr;
+    const float2 **d_tab = nullptr;  // group tasks' buffer tables
     std::vector<cudaStream_t> class_streams;
     std::vector<cudaEvent_t> class_events;
     cudaEvent_t fork_event = nullptr;
@@ -2256,6 +2257,7 @@ void destroy_conv_batch(mufft_gb_conv_batch *b)
         if (b->fork_event)
             cudaEventDestroy(b->fork_event);
         cudaFree(b->d_class);
+        cudaFree(b->d_tab);
         cudaFree(b->d_reqs);
         cudaFree(b->d_tasks);
         cudaFree(b->d_err);
@@ -2356,6 +2358,8 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
     b->small_grid = small_grid;
     cudaFree(b->d_class);
     b->d_class = nullptr;
+    cudaFree(b->d_tab);
+    b->d_tab = nullptr;
     std::vector<RaggedReq> reqs = b->sorted;
     std::vector<unsigned> split_ids, whole_ids;
     // class pipelines: (lg, stereo, zero pad) -> requests
@@ -2374,6 +2378,45 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
             whole_ids.push_back(i);
         }
     }
+    // Whole requests of sizes whose tile holds several transforms run in
+    // groups: up to that many requests of one class per task, their buffers
+    // in tables.  Work items keep the longest-first order.
+    std::vector<RaggedTask> whole;
+    std::vector<const float2 *> tab;
+    {
+        std::map<std::tuple<unsigned, unsigned, unsigned>, std::vector<unsigned>> open;
+        auto flush = [&](std::vector<unsigned> &g) {
+            RaggedTask t{g[0], kRaggedGroupTask, (unsigned short)g.size(), 0, (unsigned)tab.size()};
+            for (unsigned r : g)
+                tab.push_back(reqs[r].in);
+            for (unsigned r : g)
+                tab.push_back(reqs[r].h);
+            for (unsigned r : g)
+                tab.push_back(reqs[r].out);
+            for (unsigned r : g)
+                tab.push_back(reqs[r].spec);
+            whole.push_back(t);
+            g.clear();
+        };
+        for (unsigned r : whole_ids) {
+            const unsigned gs = ragged_group_size(reqs[r].lg);
+            if (gs <= 1) {
+                whole.push_back(RaggedTask{r, 0, 0, 0, 0});
+                continue;
+            }
+            std::vector<unsigned> &g = open[std::make_tuple(reqs[r].lg, reqs[r].stereo, reqs[r].zero_pad)];
+            g.push_back(r);
+            if (g.size() == gs)
+                flush(g);
+        }
+        for (auto &kv : open)
+            if (!kv.second.empty())
+                flush(kv.second);
+        // longest first (requests arrive sorted by cost; a group costs about one member)
+        std::stable_sort(whole.begin(), whole.end(), [&](const RaggedTask &x, const RaggedTask &y) {
+            return reqs[x.req].lg > reqs[y.req].lg;
+        });
+    }
     // phase-major over split requests, with whole requests (longest first) in between
     std::vector<RaggedTask> tasks;
     size_t w = 0;
@@ -2385,9 +2428,9 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
             for (unsigned t = 0; t < ragged_phase_tasks(reqs[r].lg, phase); t++)
                 tasks.push_back(RaggedTask{r, (unsigned short)phase, (unsigned short)t, before, 0});
         }
-        const size_t take = phase == 4 ? whole_ids.size() - w : (whole_ids.size() - w) / (5 - phase);
+        const size_t take = phase == 4 ? whole.size() - w : (whole.size() - w) / (5 - phase);
         for (size_t k = 0; k < take; k++, w++)
-            tasks.push_back(RaggedTask{whole_ids[w], 0, 0, 0, 0});
+            tasks.push_back(whole[w]);
     }
     b->args.count = (unsigned)tasks.size();
     std::vector<ClassEntry> entries;
@@ -2414,6 +2457,12 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
          !cuda_ok(cudaMemcpy(b->d_class, entries.data(), entries.size() * sizeof(ClassEntry), cudaMemcpyHostToDevice),
                   "cudaMemcpy(classes)")))
         return false;
+    if (!tab.empty() &&
+        (!cuda_ok(cudaMalloc(&b->d_tab, tab.size() * sizeof(float2 *)), "cudaMalloc(group tables)") ||
+         !cuda_ok(cudaMemcpy(b->d_tab, tab.data(), tab.size() * sizeof(float2 *), cudaMemcpyHostToDevice),
+                  "cudaMemcpy(group tables)")))
+        return false;
+    b->args.tab = b->d_tab;
     if (!cuda_ok(cudaMalloc(&b->d_tasks, std::max<size_t>(1, tasks.size()) * sizeof(RaggedTask)), "cudaMalloc(tasks)") ||
         !cuda_ok(cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(RaggedTask), cudaMemcpyHostToDevice),
                  "cudaMemcpy(tasks)") ||

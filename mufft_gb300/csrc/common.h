@@ -79,6 +79,11 @@ struct TileArgs {
     // multiply epilogue (class pipelines): output k of transform t times
     // scale * in2[t*in2_dist + k*in2_stride]
     long long in2_dist, in2_stride;
+    // per-transform buffers (tile_body with TAB): transform t reads in_tab[t]
+    // (and in2_tab[t]) and writes out_tab[t]; in_dist / out_dist are then 0
+    const float2 *const *in_tab;
+    const float2 *const *in2_tab;
+    float2 *const *out_tab;
     // one in2 for the whole batch (a filter spectrum shared by many signals):
     // bit 0 -- not offset by the grid row's batch (multi-pass passes), bit 1 --
     // not offset by the transform index (single-pass batched tiles)

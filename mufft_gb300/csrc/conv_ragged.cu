@@ -80,6 +80,50 @@ __device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, 
     __syncthreads();
 }
 
+// A group of n whole requests of one class: the n transforms of one tile pair
+// (the tile's C transforms each take one request's buffers from the tables).
+template <int L>
+__device__ void conv_group(const RaggedReq &q, const float2 *const *tab, unsigned n, float2 *smem, const float2 *tw,
+                           const float2 *rtw_fwd, const float2 *rtw_inv)
+{
+    constexpr int C = single_c<L>(), R = single_r<L>();
+    const bool mono = q.stereo == 0;
+    const float2 *const *t_in = tab, *const *t_h = tab + n;
+    float2 *const *t_out = (float2 *const *)(tab + 2 * n), *const *t_spec = (float2 *const *)(tab + 3 * n);
+    TileArgs f{};
+    f.in = q.in;
+    f.out = q.spec;
+    f.in_tab = t_in;
+    f.out_tab = t_spec;
+    f.in_stride = f.out_stride = 1;
+    f.ntrans = n;
+    f.half = q.zero_pad;
+    f.epilogue = mono ? EPI_R2C : EPI_PLAIN;
+    f.tw = tw;
+    f.rtw = rtw_fwd;
+    f.scale = 1.0f;
+    tile_body<L, R, C, 1, ALONG, ALONG, false, false, false, false, false, true>(f, 0, 0, 0, 0, smem);
+    __syncthreads();  // spectra complete and visible to the whole CTA
+
+    TileArgs b{};
+    b.in = q.spec;
+    b.in2 = q.h;
+    b.out = q.out;
+    b.in_tab = (const float2 *const *)t_spec;
+    b.in2_tab = t_h;
+    b.out_tab = t_out;
+    b.in_stride = b.out_stride = 1;
+    b.ntrans = n;
+    b.prologue = mono ? PRO_MUL_C2R : PRO_MUL;
+    b.mirror_len = L;
+    b.rtw = rtw_inv;
+    b.scale = q.scale;
+    b.conj = 3;
+    b.tw = tw;
+    tile_body<L, R, C, 1, ALONG, ALONG, true, false, false, false, false, true>(b, 0, 0, 0, 0, smem);
+    __syncthreads();
+}
+
 // Multiply phase of the four-step path on the transposed spectrum, for the
 // chunk `chunk` of `nchunks` (pairs k, L-k for mono; elements for stereo).
 template <int L1, int L2>
@@ -275,6 +319,22 @@ __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedAr
                 atomicAdd(&args.counters[q.counter], 1u);
             continue;
         }
+        if (task.phase == kRaggedGroupTask) {
+            const float2 *const *tab = args.tab + task.pad;
+            switch (q.lg) {
+            case 4: conv_group<16>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 5: conv_group<32>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 6: conv_group<64>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 7: conv_group<128>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 8: conv_group<256>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 9: conv_group<512>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 10: conv_group<1024>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 11: conv_group<2048>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            case 12: conv_group<4096>(q, tab, task.index, smem, args.tw, rf, ri); break;
+            default: break;
+            }
+            continue;
+        }
         switch (q.lg) {
         case 4: conv_single<16>(q, smem, args.tw, rf, ri); break;
         case 5: conv_single<32>(q, smem, args.tw, rf, ri); break;
@@ -291,6 +351,22 @@ __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedAr
         case 16: conv_multi<256, 256>(q, smem, args.tw, rf, ri); break;
         default: break;
         }
+    }
+}
+
+unsigned ragged_group_size(unsigned lg)
+{
+    switch (lg) {
+    case 4: return single_c<16>();
+    case 5: return single_c<32>();
+    case 6: return single_c<64>();
+    case 7: return single_c<128>();
+    case 8: return single_c<256>();
+    case 9: return single_c<512>();
+    case 10: return single_c<1024>();
+    case 11: return single_c<2048>();
+    case 12: return single_c<4096>();
+    default: return 1;
     }
 }
 

@@ -24,11 +24,19 @@ struct RaggedReq {
 // Work item: a whole request, or one task of a phase of a split request.
 struct RaggedTask {
     unsigned req;
-    unsigned short phase;  // split: 0 F1 columns, 1 F2 rows, 2 multiply, 3 I1 rows, 4 I2 columns
-    unsigned short index;  // tile / chunk within the phase
+    unsigned short phase;  // split: 0 F1 columns, 1 F2 rows, 2 multiply, 3 I1 rows, 4 I2 columns;
+                           // kRaggedGroupTask: a group of whole requests of one class
+    unsigned short index;  // tile / chunk within the phase; group: member count
     unsigned wait;         // tasks of this request that must be complete first
-    unsigned pad;
+    unsigned pad;          // group: offset of its buffer tables in RaggedArgs::tab
 };
+
+// A group task runs up to C whole requests of one (size, method, zero-pad)
+// class as the C transforms of one tile pair (C = the tile's transforms for
+// that size); `req` is its first member.  Its tables in RaggedArgs::tab: count
+// input, filter-spectrum, output and spectrum-scratch pointers, in that order.
+constexpr unsigned short kRaggedGroupTask = 8;
+unsigned ragged_group_size(unsigned lg);  // members per group task (1: whole requests run alone)
 
 // Phase task counts of a split request of length 2^lg (four-step L1 x L2).
 constexpr unsigned kRaggedMulChunks = 8;
@@ -45,6 +53,7 @@ struct RaggedArgs {
     const float2 *tw;         // stage twiddle table
     const float2 *rtw;        // per size: r2c fix-up twiddles (L) then c2r ones (L)
     unsigned rtw_off[17];     // offset of size 2^lg in rtw
+    const float2 *const *tab; // group tasks' buffer tables
 };
 
 const void *conv_ragged_fn();

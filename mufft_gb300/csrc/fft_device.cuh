@@ -624,8 +624,10 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // tiles; the caller checked load_stage0_c2r_rows's conditions).
 // EMUL: plain epilogue multiplied by scale * in2[tr*in2_dist + k*in2_stride]
 // (the spectral multiply of a convolution, fused into the forward pass).
+// TAB: every transform of the tile has its own buffers (in_tab / in2_tab /
+// out_tab, distances 0): a tile of C unrelated requests of one size.
 template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false, bool PRE = false,
-          bool C2RS = false, bool EMUL = false>
+          bool C2RS = false, bool EMUL = false, bool TAB = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
                                           float2 *smem, const float2 *sin = nullptr, unsigned twy = 0,
                                           const float2 *pre = nullptr)
@@ -640,6 +642,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     const float2 *in = a.in + ioff;
     const float2 *in2 = a.in2 ? a.in2 + ((a.in2_bcast & 1) ? 0 : ioff) : nullptr;
     float2 *out = a.out + ooff;
+    static_assert(!TAB || (Q == 1 && LMAP == ALONG && SMAP == ALONG), "per-transform buffers: row tiles");
     const unsigned tile0 = tile * C;
 
     static_assert(tile_smem_bytes<L, R, C, Q, LMAP, SMAP>() <= kMaxSmemPerCta, "tile exceeds shared memory");
@@ -686,6 +689,11 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         static_assert(LMAP == ALONG && Q == 1 && NST > 1, "staged c2r rows need a row tile with an exchange");
         load_stage0_c2r_rows<L, R, COH>(a, in, in2, tile0 + c, tl, smem + c * RS, v);
         __syncthreads();  // the exchange slices are free again
+    } else if constexpr (TAB) {
+        const unsigned t = tile0 + c;
+        const bool ok = t < a.ntrans;
+        load_stage0<L, R, Q, LMAP, COH>(a, ok ? a.in_tab[t] : in, (ok && a.in2_tab) ? a.in2_tab[t] : in2, t, j, tl,
+                                        v);
     } else {
         load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
     }
@@ -701,6 +709,10 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     const bool valid = tr < a.ntrans;
     const long long obase = (long long)tr * a.out_dist;
     const int p0 = j * BL + tl;
+    if constexpr (TAB) {
+        if (valid)
+            out = a.out_tab[tr];
+    }
 
     if (a.epilogue == EPI_R2C || a.epilogue == EPI_R2C_FULL) {
         // Z[k] and Z[L-k] sit in different threads (and CTAs): scatter the

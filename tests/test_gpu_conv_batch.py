@@ -235,3 +235,23 @@ def test_conv_batch_class_pipelines(gpu, ora, torch, classes):
     for i, ((N, method), got) in enumerate(zip(specs, outs)):
         assert rel_l2(got, ora.conv(bt.a[i], bt.b[i], N, method)) <= REL_L2_TOL, (i, N, method, classes)
         assert np.array_equal(got.view(np.uint32), again[i].view(np.uint32))
+
+
+def test_conv_batch_groups_of_small_requests(gpu, ora, torch):
+    """Many requests of one class run in groups (one tile transform per
+    request, buffers from tables): full groups and a ragged last group, two
+    classes interleaved, against the oracle."""
+    specs = []
+    for i in range(150):
+        specs.append((256, 0 if i % 3 else PAD1))           # mono, two zero-pad classes
+        specs.append((512, STEREO if i % 2 else STEREO | PAD1))
+    specs += [(32, 0), (16, STEREO), (8192, 0), (4096, STEREO)]
+    bt = Batch(gpu, torch, specs, 97000)
+    try:
+        outs = bt.run(torch)
+        again = bt.run(torch)
+    finally:
+        bt.free()
+    for i, ((N, method), got) in enumerate(zip(specs, outs)):
+        assert rel_l2(got, ora.conv(bt.a[i], bt.b[i], N, method)) <= REL_L2_TOL, (i, N, method)
+        assert np.array_equal(got.view(np.uint32), again[i].view(np.uint32))
