@@ -2319,12 +2319,13 @@ bool enqueue_class(mufft_gb_conv_batch *b, unsigned lg, bool stereo, bool zp, co
         if (phase == 2 && stereo)
             continue;
         if (phase == 2) {
+            // mono: r2c pairs, multiply, c2r pairs (stereo classes did it in F2)
             const unsigned l1 = ilog2u((unsigned)L1), l2 = ilog2u((unsigned)L2);
-            int st_ = stereo ? 1 : 0;
-            float scale = 1.0f / (float)(stereo ? L : 2 * L);
+            float scale = 1.0f / (float)(2 * L);
             const float2 *rf = b->d_rtw + b->args.rtw_off[lg], *ri = rf + L;
-            void *args[] = {(void *)&tab, (void *)&l1, (void *)&l2, &st_, &scale, (void *)&rf, (void *)&ri};
-            e = cudaLaunchKernel(class_multiply_fn(), dim3((unsigned)(L / 2048), K), dim3(256), args, 0, st);
+            void *args[] = {(void *)&tab, (void *)&l1, (void *)&l2, &scale, (void *)&rf, (void *)&ri};
+            e = cudaLaunchKernel(class_multiply_fn(), dim3((unsigned)(L1 / 32), (unsigned)(L2 / 64), K), dim3(256), args,
+                                 0, st);
         } else {
             const ClassTile &t = (phase == 0 || phase == 4) ? ct : (phase == 1 && stereo ? rmt : rt);
             const unsigned tiles = (phase == 0 || phase == 4) ? (unsigned)(L2 / t.C) : (unsigned)(L1 / t.C);

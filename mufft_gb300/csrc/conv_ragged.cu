@@ -428,43 +428,63 @@ __global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L
     tile_body<L, 16, C, 1, ALONG, ALONG, false, false, false, false, true>(a, blockIdx.x, 0, 0, 0, smem);
 }
 
-// The multiply phase for a table of requests (blockIdx.y), on the transposed
-// spectrum X^T[k1][k2] = X[k1 + L1*k2] of L = L1 x L2 points, as
-// conv_multiply above.
-__global__ void __launch_bounds__(256) class_multiply(const ClassEntry *tab, unsigned l1, unsigned l2, int stereo,
-                                                      float scale, const float2 *rtw_fwd, const float2 *rtw_inv)
+// The multiply phase of a mono class (stereo classes fuse it into F2), on the
+// transposed spectrum X^T[k1][k2] = X[k1 + L1*k2] of the packed reals (as
+// conv_multiply above): the r2c pair X[k], X[L-k] sits in rows k1 and L1-k1
+// (row 0 pairs with itself, column L2-k2).  A CTA takes 32 rows x 32 columns
+// of the lower half (k2 < L2/2, i.e. k < L/2) of request blockIdx.z and the
+// mirror elements, staged in shared memory by row-contiguous loads; the
+// filter spectrum and the twiddle tables, indexed by k, are then read along
+// k1 -- contiguously too.  k = 0 (paired with X[L]) and the self-mirrored
+// k = L/2 (row 0, column L2/2) are the special cases.
+__global__ void __launch_bounds__(256) class_multiply(const ClassEntry *tab, unsigned l1, unsigned l2, float scale,
+                                                      const float2 *rtw_fwd, const float2 *rtw_inv)
 {
-    const ClassEntry e = tab[blockIdx.y];
+    __shared__ float2 lo[32][33], hi[32][33];
+    const ClassEntry e = tab[blockIdx.z];
     const int L1 = 1 << l1, L2 = 1 << l2, L = L1 * L2;
     float2 *s = e.spec;
-    const int stride = gridDim.x * blockDim.x;
-    if (stereo) {
-        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < L; idx += stride) {
-            const int k = (idx >> l2) + L1 * (idx & (L2 - 1));
-            s[idx] = cscale(cmul(s[idx], __ldg(&e.h[k])), scale);
-        }
-        return;
+    const int a = blockIdx.x * 32, b = blockIdx.y * 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    auto mirror = [&](int k1, int k2) { return k1 == 0 ? ((L2 - k2) & (L2 - 1)) : (L1 - k1) * L2 + (L2 - 1 - k2); };
+    for (int i = w; i < 32; i += 8) {
+        lo[i][lane] = s[(a + i) * L2 + b + lane];
+        hi[i][lane] = s[mirror(a + i, b + lane)];
     }
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= L / 2; k += stride) {
+    __syncthreads();
+    for (int jj = w; jj < 32; jj += 8) {
+        const int k = a + lane + L1 * (b + jj);
         if (k == 0) {
-            const float2 z0 = s[0];
+            // s[0] holds Z[0]: X[0] and X[L] from its real and imaginary parts
+            const float2 z0 = lo[lane][jj];
             const float2 x0 = make_float2(z0.x + z0.y, 0.f), xm = make_float2(z0.x - z0.y, 0.f);
             const float2 y0 = cscale(cmul(x0, __ldg(&e.h[0])), scale);
             const float2 ym = cscale(cmul(xm, __ldg(&e.h[L])), scale);
-            s[0] = c2r_fixup(y0, ym, __ldg(&rtw_inv[0]));
+            lo[lane][jj] = hi[lane][jj] = c2r_fixup(y0, ym, __ldg(&rtw_inv[0]));  // both name s[0]
             continue;
         }
         const int km = L - k;
-        const int ik = ((k & (L1 - 1)) << l2) + (k >> l1), im = ((km & (L1 - 1)) << l2) + (km >> l1);
-        const float2 zk = s[ik], zm = s[im];
+        const float2 zk = lo[lane][jj], zm = hi[lane][jj];
         float2 xk, xk_hi, xm, xm_hi;
         r2c_bins(zk, zm, __ldg(&rtw_fwd[k]), xk, xk_hi);
         r2c_bins(zm, zk, __ldg(&rtw_fwd[km]), xm, xm_hi);
         const float2 yk = cscale(cmul(xk, __ldg(&e.h[k])), scale);
         const float2 ym = cscale(cmul(xm, __ldg(&e.h[km])), scale);
-        s[ik] = c2r_fixup(yk, ym, __ldg(&rtw_inv[k]));
-        if (km != k)
-            s[im] = c2r_fixup(ym, yk, __ldg(&rtw_inv[km]));
+        lo[lane][jj] = c2r_fixup(yk, ym, __ldg(&rtw_inv[k]));
+        hi[lane][jj] = c2r_fixup(ym, yk, __ldg(&rtw_inv[km]));
+    }
+    __syncthreads();
+    for (int i = w; i < 32; i += 8) {
+        s[(a + i) * L2 + b + lane] = lo[i][lane];
+        s[mirror(a + i, b + lane)] = hi[i][lane];
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        const int k = L / 2, idx = L2 / 2;  // row 0, column L2/2: X[L/2] pairs with itself
+        const float2 zk = s[idx];
+        float2 xk, xk_hi;
+        r2c_bins(zk, zk, __ldg(&rtw_fwd[k]), xk, xk_hi);
+        const float2 yk = cscale(cmul(xk, __ldg(&e.h[k])), scale);
+        s[idx] = c2r_fixup(yk, yk, __ldg(&rtw_inv[k]));
     }
 }
 

@@ -82,7 +82,9 @@ ClassTile class_row_tile(int L2);
 // const ClassEntry *tab, int phase) with the template's in2_dist = 1,
 // in2_stride = L1 and scale = 1 / L; the multiply launch is then skipped.
 ClassTile class_row_mul_tile(int L2);
-const void *class_multiply_fn();  // kernel(const ClassEntry *tab, unsigned l1, unsigned l2, int stereo, float scale,
-                                  //        const float2 *rtw_fwd, const float2 *rtw_inv)
+// Multiply phase of a mono class: kernel(const ClassEntry *tab, unsigned l1,
+// unsigned l2, float scale, const float2 *rtw_fwd, const float2 *rtw_inv),
+// grid (L1/32, L2/64, requests), 256 threads.
+const void *class_multiply_fn();
 
 }  // namespace mgb
