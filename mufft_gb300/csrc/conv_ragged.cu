@@ -335,16 +335,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedAr
             }
             continue;
         }
+        // whole requests up to 4096 points always come as group tasks (above)
         switch (q.lg) {
-        case 4: conv_single<16>(q, smem, args.tw, rf, ri); break;
-        case 5: conv_single<32>(q, smem, args.tw, rf, ri); break;
-        case 6: conv_single<64>(q, smem, args.tw, rf, ri); break;
-        case 7: conv_single<128>(q, smem, args.tw, rf, ri); break;
-        case 8: conv_single<256>(q, smem, args.tw, rf, ri); break;
-        case 9: conv_single<512>(q, smem, args.tw, rf, ri); break;
-        case 10: conv_single<1024>(q, smem, args.tw, rf, ri); break;
-        case 11: conv_single<2048>(q, smem, args.tw, rf, ri); break;
-        case 12: conv_single<4096>(q, smem, args.tw, rf, ri); break;
         case 13: conv_single<8192>(q, smem, args.tw, rf, ri); break;
         case 14: conv_single<16384>(q, smem, args.tw, rf, ri); break;
         case 15: conv_multi<128, 256>(q, smem, args.tw, rf, ri); break;
