@@ -235,3 +235,37 @@ def test_multipass_schedules(lib):
         lib.gb_set_fused_passes(0)
     s = _sched(lib, 1 << 21, 1)  # r2c of 2^21 reals = 2^20 complex + in-place fix-up
     assert s.split("; ")[-1].startswith("r2c_fixup")
+
+
+def test_schedule_options_in_dry_runs(lib):
+    """Resident-CTA caps pad the tile launches' shared memory; streaming row
+    tiles run as a persistent grid (both measured slower on GB300, off by
+    default); the defaults are restored."""
+    try:
+        assert lib.gb_set_tile_occupancy(2) == 0
+        s = _sched(lib, 1024, 0, batch=4096)
+        assert "smem=115712" in s, s          # (233472 / 2 - 1024) rounded to 128 bytes
+        assert lib.gb_set_tile_occupancy(0) == 0
+        assert lib.gb_set_stream_tiles(1) == 0
+        s = _sched(lib, 1024, 0, batch=4096)
+        assert "tile+stream" in s and "grid=152x1" in s, s
+    finally:
+        lib.gb_set_tile_occupancy(0)
+        lib.gb_set_stream_tiles(0)
+    s = _sched(lib, 1024, 0, batch=4096)
+    assert "+stream" not in s and "smem=34816" in s
+    for bad in (lambda: lib.gb_set_tile_occupancy(-1), lambda: lib.gb_set_tile_occupancy(33),
+                lambda: lib.gb_set_stream_tiles(2), lambda: lib.gb_set_stream_conv_fused(3),
+                lambda: lib.gb_set_stream_conv_ranges(1 << 21)):
+        assert bad() == -1
+        lib.gb_clear_error()
+
+
+def test_batched_convolution_entry_points_validate_on_host(lib):
+    assert lib.gb_execute_conv_output_batched(None, None, 0, None, 0, None, 1, None) == -1
+    lib.gb_clear_error()
+    assert lib.gb_conv_adjoint(None, None, None, 0, None, 0, None, 0, None, 1, None) == -1
+    lib.gb_clear_error()
+    assert lib.gb_stream_conv_ranges(None) == 0 and lib.gb_stream_conv_fused(None) == 0
+    assert lib.gb_stream_conv_status(None) == -1
+    lib.gb_clear_error()
