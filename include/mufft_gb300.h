@@ -224,7 +224,8 @@ void mufft_gb_free_stream_conv(mufft_gb_stream_conv *conv);
 /* Partition ranges the multiply-accumulate of convolvers created afterwards
  * splits the P partitions into (each range a row of CTAs whose partial sums
  * are added in range order); 0, the default, sizes it to the GPU.  Values
- * above P are clamped to P. */
+ * are clamped to the partitions (P, or P - 1 for one-launch blocks, which
+ * also keep every CTA resident at once). */
 int mufft_gb_set_stream_conv_ranges(unsigned ranges);
 /* Partition ranges a convolver uses. */
 unsigned mufft_gb_stream_conv_ranges(const mufft_gb_stream_conv *conv);
