@@ -236,9 +236,19 @@ unsigned mufft_gb_stream_conv_ranges(const mufft_gb_stream_conv *conv);
  * launches (0).  mufft_gb_stream_conv_fused reports which a convolver uses. */
 int mufft_gb_set_stream_conv_fused(int enable);
 int mufft_gb_stream_conv_fused(const mufft_gb_stream_conv *conv);
-/* Synchronises the device; nonzero if a block launch's bounded wait timed
- * out since the last call (its output block is then not valid). */
+/* Synchronises the device; MUFFT_GB_ERR_UNSUPPORTED if a one-launch block's
+ * bounded wait timed out since the last call (clearing the flag).  The
+ * output of that block and the convolver's input history are then not
+ * valid: call mufft_gb_stream_conv_reset before relying on further output.
+ * The launches themselves stay consistent, so processing may simply go on
+ * after the reset. */
 int mufft_gb_stream_conv_status(mufft_gb_stream_conv *conv);
+/* For testing a caller's error handling: while enabled (1), every block
+ * launch waits for a spectrum flag that is never published, gives up after
+ * well under a millisecond and reports the timeout through
+ * mufft_gb_stream_conv_status; 0 restores normal operation.  One-launch
+ * convolvers only (MUFFT_GB_ERR_UNSUPPORTED otherwise). */
+int mufft_gb_stream_conv_inject_timeout(mufft_gb_stream_conv *conv, int enable);
 
 /* ------------------------------------------------- allocation-free execute */
 
@@ -251,12 +261,14 @@ int mufft_gb_stream_conv_status(mufft_gb_stream_conv *conv);
  * library (2^20 points of scratch, about 8.6 MB per GPU, held until exit).
  *   N: power of two, 2 <= N <= 2^20 (1048576); larger N returns
  *      MUFFT_GB_ERR_UNSUPPORTED -- use a plan.
- *   output, input: device-accessible, N complex each, not overlapping
- *      (host memory returns MUFFT_GB_ERR_HOST_POINTER).
+ *   output, input: N complex each in device or managed memory, or in
+ *      page-locked host memory mapped into the device's address space (other
+ *      host memory returns MUFFT_GB_ERR_HOST_POINTER).  output == input
+ *      transforms in place; partially overlapping buffers are not allowed.
  *   stream: cudaStream_t (NULL = legacy default stream); enqueued, not synchronised.
  * The first call on a device sets up (looks up the arrays' device addresses,
  * fills the twiddle table, synchronises the device): make it before any
- * stream capture.  All calls on a device share one scratch array, which keeps
+ * stream capture.  Later calls take no lock.  All calls on a device share one scratch array, which keeps
  * the last call's contents; calls whose kernels overlap on the GPU race on it,
  * so serialise them (one stream).  Returns MUFFT_GB_OK or an error code. */
 int mufft_gb_execute_c2c_noalloc(unsigned N, int direction, void *output, const void *input, void *stream);

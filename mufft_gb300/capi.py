@@ -112,6 +112,7 @@ GB_H = [
     ("set_stream_conv_fused", _i, [_i]),
     ("stream_conv_fused", _i, [_vp]),
     ("stream_conv_status", _i, [_vp]),
+    ("stream_conv_inject_timeout", _i, [_vp, _i]),
     ("free_stream_conv", None, [_vp]),
     ("create_conv_batch", _vp, [_vp, _u, _u]),
     ("execute_conv_batch", _i, [_vp, _vp]),

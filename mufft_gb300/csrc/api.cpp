@@ -2891,6 +2891,8 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
         a.tickets = c->counter;
         a.err = c->err;
         a.s = 1.0f / (float)L;
+        a.wait_polls = kUpolsWaitPolls;
+        a.wait_skew = 0;
         return c;
     }
     cudaGraph_t gr = nullptr;
@@ -2990,6 +2992,21 @@ int mufft_gb_set_stream_conv_fused(int enable)
 }
 
 int mufft_gb_stream_conv_fused(const mufft_gb_stream_conv *c) { return c && c->M ? 1 : 0; }
+
+int mufft_gb_stream_conv_inject_timeout(mufft_gb_stream_conv *c, int enable)
+{
+    if (!c || enable < 0 || enable > 1) {
+        set_error(MUFFT_GB_ERR_INVALID, "null convolver or enable not 0 / 1");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (!c->M) {
+        set_error(MUFFT_GB_ERR_UNSUPPORTED, "only one-launch blocks wait on other CTAs");
+        return MUFFT_GB_ERR_UNSUPPORTED;
+    }
+    c->block_args.wait_skew = enable ? 1u : 0u;
+    c->block_args.wait_polls = enable ? kUpolsInjectedWaitPolls : kUpolsWaitPolls;
+    return MUFFT_GB_OK;
+}
 
 int mufft_gb_stream_conv_status(mufft_gb_stream_conv *c)
 {
@@ -3383,8 +3400,23 @@ void *mufft_calloc(size_t size)
 
 void mufft_free(void *ptr)
 {
-    if (ptr)
-        cudaFreeHost(ptr);
+    if (!ptr)
+        return;
+    // mufft_alloc memory is page-locked host memory; anything else a caller
+    // passes (malloc memory, as the reference's mufft_free accepts, or device
+    // memory) goes back where it came from
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        free(ptr);
+        return;
+    }
+    switch (at.type) {
+    case cudaMemoryTypeHost: cudaFreeHost(ptr); break;
+    case cudaMemoryTypeDevice:
+    case cudaMemoryTypeManaged: cudaFree(ptr); break;
+    default: free(ptr); break;
+    }
 }
 
 void *mufft_gb_device_alloc(size_t size)

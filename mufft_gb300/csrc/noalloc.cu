@@ -26,6 +26,7 @@
 //     any stream capture.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <mutex>
 
@@ -63,7 +64,7 @@ __global__ void noalloc_fill_twiddles(float2 *t)
 }
 
 struct NoAllocDevice {
-    bool ready = false;
+    std::atomic<bool> ready{false};  // set (release) once the fields below are final
     float2 *scratch = nullptr;   // device address of g_noalloc_scratch
     float2 *twiddles = nullptr;  // device address of g_noalloc_twiddles
     // per log2(N): single-pass tile, or the two four-step tiles
@@ -115,7 +116,7 @@ int set_up(int dev)
         e = cudaDeviceSynchronize();
     if (e != cudaSuccess)
         return (int)e;
-    d.ready = true;
+    d.ready.store(true, std::memory_order_release);
     return MUFFT_GB_OK;
 }
 
@@ -126,14 +127,21 @@ cudaError_t launch(const TileKernel *k, TileArgs &a, unsigned ntrans, cudaStream
                             a.tw_lo ? k->smem : k->smem_ex, st);
 }
 
-bool device_pointer(const void *p)
+// The address kernels use for p: p itself for device and managed memory, the
+// mapped device address for page-locked host memory mapped into the device's
+// address space; null for memory the device cannot reach.
+const void *device_address(const void *p)
 {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return nullptr;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)
+        return p;
+    if (at.type == cudaMemoryTypeHost && at.devicePointer)
+        return at.devicePointer;
+    return nullptr;
 }
 
 }  // namespace
@@ -149,7 +157,9 @@ extern "C" int mufft_gb_execute_c2c_noalloc(unsigned N, int direction, void *out
         return MUFFT_GB_ERR_INVALID;
     if (N > kNoAllocMaxPoints)
         return MUFFT_GB_ERR_UNSUPPORTED;  // beyond the fixed scratch: use a plan
-    if (!device_pointer(input) || !device_pointer(output))
+    input = device_address(input);
+    output = const_cast<void *>(device_address(output));
+    if (!input || !output)
         return MUFFT_GB_ERR_HOST_POINTER;
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -158,9 +168,10 @@ extern "C" int mufft_gb_execute_c2c_noalloc(unsigned N, int direction, void *out
     if (dev < 0 || dev >= kMaxDev)
         return MUFFT_GB_ERR_UNSUPPORTED;
     NoAllocDevice &d = g_noalloc[dev];
-    {
+    if (!d.ready.load(std::memory_order_acquire)) {
+        // first call on this device only: later calls take no lock
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!d.ready) {
+        if (!d.ready.load(std::memory_order_relaxed)) {
             int rc = set_up(dev);
             if (rc != MUFFT_GB_OK)
                 return rc;

@@ -14,7 +14,10 @@
 //
 // Only a group's finishing CTA waits, and only for CTA 0, which waits for
 // nobody; the grid is sized so that all CTAs are resident together.  The wait
-// is bounded: on timeout the CTA records an error and skips the group.
+// is bounded: on timeout the CTA records an error and leaves the group's
+// output and delay-line bins unwritten, but still does the group's ticket
+// bookkeeping (and, if it is the last group, the inverse transform and the
+// block count), so the next launch starts from consistent tickets.
 //   tickets[0] = k, [1] groups finished, [2] = k + 1 once the spectrum of
 //   block k is out, [3 + x] range CTAs done with group x.
 #include "fft_device.cuh"
@@ -145,17 +148,18 @@ __global__ void __launch_bounds__(256) upols_block(const UpolsBlockArgs a)
     red[w][lane] = t;  // red was last read before the ticket
     if (threadIdx.x == 0) {
         // the current spectrum (CTA 0, which waits for nobody)
-        unsigned i = 0;
-        while (ld_acquire(&a.tickets[2]) != k + 1 && ++i < (1u << 24))
+        const unsigned want = k + 1 + a.wait_skew;
+        bool seen = ld_acquire(&a.tickets[2]) == want;
+        for (unsigned i = 0; !seen && i < a.wait_polls; i++) {
             __nanosleep(32);
-        ready = i < (1u << 24);
-        if (!ready)
+            seen = ld_acquire(&a.tickets[2]) == want;
+        }
+        ready = seen;
+        if (!seen)
             atomicExch(a.err, 1);
     }
     __syncthreads();
-    if (!ready)
-        return;
-    if (w == 0) {
+    if (ready && w == 0) {
         float4 r = red[0][lane];
 #pragma unroll
         for (int q = 1; q < kWarps; q++)

@@ -23,7 +23,14 @@ struct UpolsBlockArgs {
                          // [2] spectrum of block k published (k + 1), [3 + x] range CTAs done with group x
     int *err;            // set when a bounded wait for the spectrum times out
     float s;             // 1 / transform length
+    unsigned wait_polls; // bound of the wait for the spectrum (polls of ~32 ns and more)
+    unsigned wait_skew;  // 0; 1 makes the wait look for a flag value nobody publishes
+                         // (the timeout path, for tests of a caller's error handling)
 };
+// Polls of the spectrum wait before it gives up (half a second or more).
+constexpr unsigned kUpolsWaitPolls = 1u << 24;
+// The bound used while a timeout is injected: well under a millisecond.
+constexpr unsigned kUpolsInjectedWaitPolls = 4096;
 inline unsigned upols_block_tickets(unsigned groups) { return 3 + groups; }
 
 // Row-tile length M (complex points) with a compiled fused kernel, and its

@@ -48,3 +48,24 @@ def complex_logmag(seed: int, n: int, lo: float = 1e-3, hi: float = 1e3) -> np.n
     mag = np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * u[0::2])
     ph = 2.0 * np.pi * u[1::2]
     return (mag * np.exp(1j * ph)).astype(np.complex64)
+
+
+def ragged_conv_requests(seed: int = 4, count: int = 512):
+    """The ragged convolution mix: `count` requests with block size N = 2^e,
+    e uniform on 8..16 (numpy Generator `seed`), exactly count/2 of them
+    STEREO_MONO (a seeded permutation picks which); request i has an input of
+    N/2 samples (uniform [-1, 1), complex for stereo, SplitMix64 seed
+    20000 + i) and a filter of N/2 taps N(0,1) * exp(-t / (N/8)) (seed
+    10000 + i).  Returns (N, stereo, input, filter) tuples."""
+    rng = np.random.default_rng(seed)
+    e = rng.integers(8, 17, count)
+    stereo = np.zeros(count, bool)
+    stereo[rng.permutation(count)[: count // 2]] = True
+    reqs = []
+    for i in range(count):
+        N = 1 << int(e[i])
+        t = np.arange(N // 2)
+        h = (normal(10000 + i, N // 2) * np.exp(-t / (N / 8))).astype(np.float32)
+        x = complex_uniform(20000 + i, N // 2) if stereo[i] else uniform(20000 + i, N // 2)
+        reqs.append((N, bool(stereo[i]), x, h))
+    return reqs

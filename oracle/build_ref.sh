@@ -6,9 +6,13 @@
 # (CMakeLists.txt:23-63) driven by gcc directly.  Nothing is copied: the
 # sources are read where they lie.
 #
-# usage: oracle/build_ref.sh [reference_dir] [output_dir]
+# usage: oracle/build_ref.sh reference_dir [output_dir]
 set -eu
-REF=${1:-/root/reference}
+if [ $# -lt 1 ]; then
+    echo "usage: $0 reference_dir [output_dir]" >&2
+    exit 2
+fi
+REF=$1
 OUT=${2:-$(dirname "$0")/_ref}
 CC=${CC:-gcc}
 if [ ! -f "$REF/fft.c" ]; then

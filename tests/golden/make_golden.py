@@ -32,7 +32,9 @@ OUT = Path(__file__).resolve().parent / "golden.npz"
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py REFERENCE_SOURCE_DIR")
+    ref_dir = sys.argv[1]
     subprocess.run([str(ROOT / "oracle" / "build_ref.sh"), ref_dir], check=True)
     from oracle.oracle import load_reference
     ref = load_reference()

@@ -265,3 +265,140 @@ def test_batched_adjoint_rejects_bad_arguments(gpu, torch):
         gpu.gb_clear_error()
     finally:
         pl.free()
+
+
+def test_adjoint_full_workload(gpu, torch):
+    """The filter-fitting workload at full size: 64 stereo signals of 2^20
+    frames, a 2^16-tap filter (N(0,1) * exp(-t/8192)), N = 2^21 with both
+    blocks zero-padded so the circular convolution is the linear one, loss
+    0.5 * sum_b ||conv(x_b, h) - y*_b||^2 with y* made by a hidden filter.
+      1. Both GPU gradients (mufft_gb_conv_adjoint, all 64 signals) against
+         the FP64 gradient of the same loss, relative L2 <= 1e-4.
+      2. FP64 central differences of the loss (torch float64 FFTs on the GPU)
+         on 256 random filter taps and 256 random input samples.
+      3. 200 steps of gradient descent on the taps: the loss falls
+         monotonically until it reaches the FP32 floor."""
+    B, L, T = 64, 1 << 20, 1 << 16
+    N = 2 * L
+    method = STEREO | PAD1 | PAD2
+    st = _st(torch)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.zeros((B, N), dtype=torch.complex64, device="cuda")
+    x[:, :L].real.uniform_(-1, 1, generator=g)
+    x[:, :L].imag.uniform_(-1, 1, generator=g)
+    t = torch.arange(T, device="cuda", dtype=torch.float64)
+    h_hidden = torch.zeros(N, dtype=torch.float64, device="cuda")
+    h_hidden[:T] = torch.randn(T, device="cuda", generator=g, dtype=torch.float64) * torch.exp(-t / 8192)
+    h0 = torch.zeros(N, dtype=torch.float64, device="cuda")
+    h0[:T] = torch.randn(T, device="cuda", generator=g, dtype=torch.float64) * torch.exp(-t / 8192)
+
+    # FP64 spectra of the signals; targets y* = conv(x, h_hidden) rounded to complex64
+    X = torch.fft.fft(x.to(torch.complex128), dim=1)
+    ystar = torch.empty((B, N), dtype=torch.complex64, device="cuda")
+    Hh = torch.fft.fft(h_hidden)
+    for c in range(0, B, 8):
+        ystar[c:c + 8] = torch.fft.ifft(X[c:c + 8] * Hh, dim=1).to(torch.complex64)
+
+    pl = ConvPlan(gpu, N, method)
+    try:
+        # ---- 1. GPU gradients at h0 against the FP64 gradient
+        h32 = h0.to(torch.float32)
+        H = pl.spectrum(torch, K.CONV_BLOCK_SECOND, h32)
+        dA = torch.empty((B, pl.block), dtype=torch.complex64, device="cuda")
+        for b in range(B):
+            rc = gpu.gb_execute_conv_input_async(pl.p, K.CONV_BLOCK_FIRST, dA[b].data_ptr(), x[b].data_ptr(), st)
+            assert rc == 0, gpu.gb_last_error_string()
+        y = torch.empty((B, N), dtype=torch.complex64, device="cuda")
+        assert gpu.gb_execute_conv_output_batched(pl.p, y.data_ptr(), N, dA.data_ptr(), pl.block, H.data_ptr(), B,
+                                                  st) == 0, gpu.gb_last_error_string()
+        r = y - ystar
+        gh = torch.full((N,), float("nan"), dtype=torch.float32, device="cuda")
+        gx = torch.full((B, N), float("nan"), dtype=torch.complex64, device="cuda")
+        assert gpu.gb_conv_adjoint(pl.p, gh.data_ptr(), gx.data_ptr(), N, r.data_ptr(), N, dA.data_ptr(), pl.block,
+                                   H.data_ptr(), B, st) == 0, gpu.gb_last_error_string()
+        torch.cuda.synchronize()
+        del y, r
+
+        H0 = torch.fft.fft(h0)
+        gh_ref = torch.zeros(N, dtype=torch.complex128, device="cuda")
+        gx_err2, gx_ref2 = 0.0, 0.0
+        for c in range(0, B, 8):
+            R = torch.fft.fft(torch.fft.ifft(X[c:c + 8] * H0, dim=1) - ystar[c:c + 8].to(torch.complex128), dim=1)
+            gh_ref += (R * torch.conj(X[c:c + 8])).sum(dim=0)
+            gxr = torch.fft.ifft(R * torch.conj(H0), dim=1)
+            gx_err2 += float((gx[c:c + 8].to(torch.complex128) - gxr).abs().square().sum())
+            gx_ref2 += float(gxr.abs().square().sum())
+            del R, gxr
+        gh_ref = torch.fft.ifft(gh_ref).real
+        gh_rel = float(torch.linalg.norm(gh[:T].double() - gh_ref[:T]) / torch.linalg.norm(gh_ref[:T]))
+        gx_rel = (gx_err2 / gx_ref2) ** 0.5
+        assert gh_rel <= 1e-4, gh_rel
+        assert gx_rel <= 1e-4, gx_rel
+
+        # ---- 2. FP64 central differences of the loss
+        def loss_filter(hv):
+            Hv = torch.fft.fft(hv)
+            tot = 0.0
+            for c in range(0, B, 8):
+                d = torch.fft.ifft(X[c:c + 8] * Hv, dim=1) - ystar[c:c + 8].to(torch.complex128)
+                tot += 0.5 * float(d.abs().square().sum())
+            return tot
+
+        def loss_signal(b, xv):  # the one term of the sum that x_b enters
+            d = torch.fft.ifft(torch.fft.fft(xv) * H0) - ystar[b].to(torch.complex128)
+            return 0.5 * float(d.abs().square().sum())
+
+        rng = np.random.default_rng(55)
+        ghc = gh.cpu().numpy()
+        scale_h = float(np.abs(ghc[:T]).max())
+        eps = 1e-2  # the loss is quadratic: central differences carry only rounding error
+        for j in rng.choice(T, 256, replace=False):
+            e = torch.zeros(N, dtype=torch.float64, device="cuda")
+            e[int(j)] = eps
+            fd = (loss_filter(h0 + e) - loss_filter(h0 - e)) / (2 * eps)
+            assert abs(fd - ghc[j]) < 1e-4 * scale_h, ("filter", int(j), fd, float(ghc[j]))
+        gxc_rows = {}
+        for b, n in zip(rng.integers(0, B, 256), rng.integers(0, L, 256)):
+            b, n = int(b), int(n)
+            if b not in gxc_rows:
+                gxc_rows[b] = gx[b].cpu().numpy()
+            scale_x = float(np.abs(gxc_rows[b][:L]).max())
+            xb = x[b].to(torch.complex128)
+            fd = 0j
+            for unit in (1.0, 1j):
+                e = torch.zeros(N, dtype=torch.complex128, device="cuda")
+                e[n] = eps * unit
+                d = (loss_signal(b, xb + e) - loss_signal(b, xb - e)) / (2 * eps)
+                fd += d * unit
+            assert abs(fd - gxc_rows[b][n]) < 1e-4 * scale_x, ("input", b, n, fd, gxc_rows[b][n])
+        del gx
+
+        # ---- 3. 200 descent steps on the taps, from zero
+        spec_power = torch.zeros(N, dtype=torch.float64, device="cuda")
+        for c in range(0, B, 8):
+            spec_power += X[c:c + 8].abs().square().sum(dim=0)
+        lr = 1.0 / float(spec_power.max())
+        del X
+        torch.cuda.empty_cache()
+        h = torch.zeros(N, dtype=torch.float32, device="cuda")
+        y = torch.empty((B, N), dtype=torch.complex64, device="cuda")
+        losses = []
+        for step in range(200):
+            H = pl.spectrum(torch, K.CONV_BLOCK_SECOND, h)
+            assert gpu.gb_execute_conv_output_batched(pl.p, y.data_ptr(), N, dA.data_ptr(), pl.block, H.data_ptr(),
+                                                      B, st) == 0
+            y.sub_(ystar)
+            losses.append(0.5 * float(y.abs().square().sum(dtype=torch.float64)))
+            assert gpu.gb_conv_adjoint(pl.p, gh.data_ptr(), None, 0, y.data_ptr(), N, dA.data_ptr(), pl.block,
+                                       H.data_ptr(), B, st) == 0
+            h[:T].sub_(lr * gh[:T])
+        h_err = float(torch.linalg.norm(h[:T].double() - h_hidden[:T]) / torch.linalg.norm(h_hidden[:T]))
+    finally:
+        pl.free()
+    floor = 1e-9 * losses[0]
+    far = [i for i in range(1, len(losses)) if losses[i - 1] > floor]
+    assert len(far) >= 10 and all(losses[i] < losses[i - 1] for i in far), losses[:16]
+    assert losses[-1] < 1e-6 * losses[0], (losses[0], losses[-1])
+    assert h_err < 1e-3, h_err
+    print(f"full adjoint workload: grad rel L2 filter {gh_rel:.2e} input {gx_rel:.2e}; "
+          f"loss {losses[0]:.4e} -> {losses[-1]:.4e} in 200 steps; filter error {h_err:.2e}")

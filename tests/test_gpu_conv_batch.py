@@ -255,3 +255,45 @@ def test_conv_batch_groups_of_small_requests(gpu, ora, torch):
     for i, ((N, method), got) in enumerate(zip(specs, outs)):
         assert rel_l2(got, ora.conv(bt.a[i], bt.b[i], N, method)) <= REL_L2_TOL, (i, N, method)
         assert np.array_equal(got.view(np.uint32), again[i].view(np.uint32))
+
+
+def test_conv_batch_ragged_512_request_mix(gpu, ora, torch):
+    """The ragged-convolution workload itself: 512 requests, N = 2^8..2^16
+    log-uniform, 256 STEREO_MONO, N/2-sample inputs and N/2-tap decaying
+    filters with both zero-pad flags (signals.ragged_conv_requests, seed 4),
+    as one batch; every output against the oracle's full convolution
+    sequence (fft.c:794-809) at relative L2 <= 1e-5."""
+    reqs = signals.ragged_conv_requests(4, 512)
+    creq = (K.ConvRequest * len(reqs))()
+    keep, outs, full = [], [], []
+    for i, (N, stereo, x, h) in enumerate(reqs):
+        m = PAD1 | PAD2 | (STEREO if stereo else 0)
+        hp = np.zeros(N, np.float32)
+        hp[: N // 2] = h
+        xp = np.zeros(N, np.complex64 if stereo else np.float32)
+        xp[: N // 2] = x
+        H = filter_spectrum(gpu, hp, N, m)
+        din = torch.from_numpy(np.ascontiguousarray(x)).cuda()   # N/2 samples: the upper half is never read
+        dh = torch.from_numpy(H).cuda()
+        dout = torch.full((N,), float("nan"), dtype=torch.complex64 if stereo else torch.float32, device="cuda")
+        creq[i] = K.ConvRequest(N, m, din.data_ptr(), dh.data_ptr(), dout.data_ptr())
+        keep += [din, dh]
+        outs.append(dout)
+        full.append((N, m, xp, hp))
+    batch = gpu.gb_create_conv_batch(creq, len(reqs), 0)
+    assert batch, gpu.gb_last_error_string()
+    try:
+        assert gpu.gb_execute_conv_batch(batch, torch.cuda.current_stream().cuda_stream) == 0
+        torch.cuda.synchronize()
+        assert gpu.gb_conv_batch_status(batch) == 0, gpu.gb_last_error_string()
+    finally:
+        gpu.gb_free_conv_batch(batch)
+    worst = 0.0
+    for i, ((N, m, xp, hp), dout) in enumerate(zip(full, outs)):
+        got = dout.cpu().numpy()
+        want = ora.conv(xp, hp, N, m)
+        assert np.all(np.isfinite(got)), (i, N, m)
+        err = rel_l2(got, want)
+        worst = max(worst, err)
+        assert err <= REL_L2_TOL, (i, N, m, err)
+    print(f"512-request mix: worst relative L2 against the oracle {worst:.2e}")

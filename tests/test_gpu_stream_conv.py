@@ -124,3 +124,49 @@ def test_stream_conv_rejects_bad_arguments(gpu):
         assert not gpu.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0)
         assert gpu.gb_last_error() == -1
         gpu.gb_clear_error()
+
+
+@pytest.mark.parametrize("method", [0, STEREO])
+def test_stream_conv_timeout_then_reset(gpu, method):
+    """A block whose bounded wait runs out (injected: the awaited flag is
+    never published) is reported by the status call; the launches stay
+    consistent, so after a reset the stream convolves correctly again --
+    every later block, not only the first."""
+    block, taps = 512, 512 * 9 + 17
+    stereo = method & 1
+    sample = 8 if stereo else 4
+    h = (signals.normal(65000, taps) * np.exp(-np.arange(taps) / (taps / 4))).astype(np.float32)
+    x = signals.complex_uniform(65001, 14 * block) if stereo else signals.uniform(65001, 14 * block)
+    conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, taps, 0)
+    assert conv, gpu.gb_last_error_string()
+    try:
+        assert gpu.gb_stream_conv_fused(conv) == 1
+        inp, outp = gpu.gb_stream_conv_input(conv), gpu.gb_stream_conv_output(conv)
+
+        def push(blk):
+            blk = np.ascontiguousarray(blk)
+            assert gpu.gb_memcpy(inp, blk.ctypes.data, block * sample) == 0
+            assert gpu.gb_stream_conv_process(conv, None) == 0, gpu.gb_last_error_string()
+            out = np.zeros(block, np.complex64 if stereo else np.float32)
+            assert gpu.gb_memcpy(out.ctypes.data, outp, block * sample) == 0
+            return out
+
+        for k in range(3):
+            push(x[k * block:(k + 1) * block])
+        assert gpu.gb_stream_conv_status(conv) == 0
+        assert gpu.gb_stream_conv_inject_timeout(conv, 1) == 0
+        push(x[3 * block:4 * block])
+        assert gpu.gb_stream_conv_status(conv) == -2  # the timeout is reported ...
+        assert gpu.gb_stream_conv_status(conv) == 0   # ... once
+        gpu.gb_clear_error()
+        assert gpu.gb_stream_conv_inject_timeout(conv, 0) == 0
+        assert gpu.gb_stream_conv_reset(conv, None) == 0
+        rest = x[4 * block:]
+        got = np.concatenate([push(rest[k * block:(k + 1) * block]) for k in range(len(rest) // block)])
+        assert gpu.gb_stream_conv_status(conv) == 0, gpu.gb_last_error_string()
+    finally:
+        gpu.gb_free_stream_conv(conv)
+    ref = linear_conv_f64(rest, h)
+    if not stereo:
+        ref = ref.real
+    assert rel_l2(got, ref) < 1e-5
