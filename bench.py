@@ -509,9 +509,8 @@ def companion_stream_conv(lib, torch) -> dict:
     sp = torch.cuda.current_stream().cuda_stream
     res = {}
     for fused in (1, 0):
-        lib.gb_set_stream_conv_fused(fused)
-        conv = lib.gb_create_stream_conv(block, 1, h.ctypes.data, taps, 0)
-        lib.gb_set_stream_conv_fused(1)
+        opts = lib.options(stream_conv_fused=fused)
+        conv = lib.gb_create_stream_conv(block, 1, h.ctypes.data, taps, 0, ctypes.byref(opts))
         if not conv:
             raise RuntimeError(lib.gb_last_error_string().decode())
         res[fused] = (_time_ms(torch, lambda: lib.gb_stream_conv_process(conv, sp), reps=200, warm=20),
@@ -556,10 +555,9 @@ def companion_split(lib, torch) -> dict:
                    "B: magnitude log-uniform 1e-3..1e3, uniform phase (128 rows)"}
     for name, flags, engine in (("fp32", 0, 0), ("bf16x3", K.FLAG_SPLIT_BF16X3, 0), ("bf16x2", K.FLAG_SPLIT_BF16X2, 0),
                                 ("bf16x3_mma_sync", K.FLAG_SPLIT_BF16X3, 1)):
-        lib.gb_set_split_engine(engine)
-        p = lib.gb_create_plan_1d_c2c_batched(N, -1, flags, B, 0, 0)
-        ps = lib.gb_create_plan_1d_c2c_batched(N, -1, flags, sub, 0, 0)
-        lib.gb_set_split_engine(0)
+        opts = lib.options(split_engine=engine)
+        p = lib.gb_create_plan_1d(0, N, -1, flags, B, 0, 0, ctypes.byref(opts))
+        ps = lib.gb_create_plan_1d(0, N, -1, flags, sub, 0, 0, ctypes.byref(opts))
         if not p or not ps:
             raise RuntimeError(lib.gb_last_error_string().decode())
         ms = _time_ms(torch, lambda: lib.gb_execute_plan_1d_async(p, y.data_ptr(), x.data_ptr(), sp), reps=10)
@@ -608,7 +606,7 @@ def companion_ragged(lib, torch) -> dict:
         creq[i] = K.ConvRequest(N, m, din.data_ptr(), dH.data_ptr(), dout.data_ptr())
         seq.append((p, din, dH, dspec, dseq))
         algo += (14 if stereo else 8) * N
-    batch = lib.gb_create_conv_batch(creq, len(reqs), 0)
+    batch = lib.gb_create_conv_batch(creq, len(reqs), 0, None)
     if not batch:
         raise RuntimeError(lib.gb_last_error_string().decode())
 

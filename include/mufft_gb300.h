@@ -65,6 +65,79 @@ mufft_plan_1d *mufft_gb_create_plan_1d_r2c_batched(unsigned N, unsigned flags,
 mufft_plan_1d *mufft_gb_create_plan_1d_c2r_batched(unsigned N, unsigned flags,
                                                    unsigned batch, size_t idist, size_t odist);
 
+/* ------------------------------------------------------- plan options */
+
+/* Schedule choices of one plan or batch.  The reference has no global state
+ * (its choices come from CPUID and static tables, fft.c:217-435); here every
+ * choice travels with the creation call that uses it, so threads creating
+ * plans with different choices never interfere.  Initialise with
+ * mufft_gb_options_init (the defaults below), change fields, pass the
+ * address; NULL means the defaults (and, for 1D plans, the autotuner's
+ * remembered choice for the shape, see mufft_gb_autotune_1d). */
+typedef struct mufft_gb_tile_choice {
+    unsigned L;             /* transform length of the tile */
+    int load_across;        /* loads walk across neighbouring transforms (1) or along one (0) */
+    int store_across;       /* the same for stores */
+    unsigned transforms_per_tile, elems_per_thread, cluster_ctas;  /* 0 = any */
+} mufft_gb_tile_choice;
+
+#define MUFFT_GB_MAX_TILE_CHOICES 8
+
+typedef struct mufft_gb_options {
+    unsigned size;               /* sizeof(mufft_gb_options), set by mufft_gb_options_init */
+    /* 1D transforms longer than one on-chip tile (16384 points): 0 automatic,
+     * 2 four-step, 3 three-level decomposition with smaller tiles */
+    int multipass_levels;
+    /* inter-pass twiddles: -1 automatic, 0 sincospif per element, 1 FP64
+     * table times a per-tile factor, 2 per-tile column powers */
+    int twiddle_table;
+    /* three-level N1 x 65536 transforms: last two passes as one persistent
+     * launch with an L2-resident intermediate (1) or two launches (0) */
+    int fused_passes;
+    /* column passes staged by TMA: 0 off, 1 double-buffered persistent
+     * CTAs, 2 single buffer */
+    int tma;
+    /* tile passes run at most this many CTAs per SM (0 = as many as fit) */
+    int tile_occupancy;
+    /* contiguous row passes as persistent CTAs prefetching their next tile (1) */
+    int stream_tiles;
+    /* split-precision products on tcgen05.mma with TMEM (0) or mma.sync (1) */
+    int split_engine;
+    /* 2D columns: 0 automatic (8192 points and more as a two-pass four-step
+     * of short, wide column tiles), 1 one pass, 2 two passes where possible */
+    int columns_2d;
+    /* ragged convolution batches: requests of at least conv_split complex
+     * points run as phase tasks over many CTAs (0: none), of at least
+     * conv_classes points as class pipelines (0: none); powers of two in
+     * 16384..65536 */
+    unsigned conv_split, conv_classes;
+    /* streaming convolution: partition ranges of the multiply-accumulate (0
+     * sized to the GPU) and one launch per block (1) or a graph (0) */
+    unsigned stream_conv_ranges;
+    int stream_conv_fused;
+    /* preferred tile kernels (mufft_gb_list_tiles), first ntiles entries */
+    unsigned ntiles;
+    mufft_gb_tile_choice tiles[MUFFT_GB_MAX_TILE_CHOICES];
+} mufft_gb_options;
+
+/* The defaults: levels 0, twiddles -1, fused 0, tma 0, occupancy 0, stream
+ * tiles 0, split engine 0, 2D columns 0, conv_split 65536, conv_classes
+ * 16384, stream ranges 0, stream fused 1, no tile choices. */
+void mufft_gb_options_init(mufft_gb_options *opts);
+
+/* 1D plans of every kind with options: kind 0 c2c, 1 r2c, 2 c2r (direction
+ * is used by c2c only); the other arguments as the _batched creators, which
+ * are this call with opts = NULL.  Invalid options return NULL with
+ * MUFFT_GB_ERR_INVALID. */
+mufft_plan_1d *mufft_gb_create_plan_1d(int kind, unsigned N, int direction, unsigned flags, unsigned batch,
+                                       size_t idist, size_t odist, const mufft_gb_options *opts);
+/* 2D plans with options: kind 0 c2c, 1 r2c, 2 c2r, as mufft_create_plan_2d_*. */
+mufft_plan_2d *mufft_gb_create_plan_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsigned flags,
+                                       const mufft_gb_options *opts);
+/* Convolution plans with options for their inner transforms, as
+ * mufft_create_plan_conv. */
+mufft_plan_conv *mufft_gb_create_plan_conv(unsigned N, unsigned flags, unsigned method, const mufft_gb_options *opts);
+
 /* ------------------------------------------------- asynchronous execution */
 
 /* Enqueue on `stream` (a cudaStream_t; NULL = the legacy default stream)
@@ -162,23 +235,17 @@ typedef struct mufft_gb_conv_request {
 typedef struct mufft_gb_conv_batch mufft_gb_conv_batch;
 
 /* Prepares `count` requests of mixed sizes for one persistent launch,
- * captured in a CUDA graph.  Requests of 16384 complex points and more run
- * as class pipelines (mufft_gb_set_conv_classes); the rest, longest first,
- * in a persistent kernel, whole in one CTA each or -- from the split size --
- * as phase tasks spread over many CTAs.  flags: 0, or MUFFT_GB_FLAG_AUTOTUNE
- * to time the batch with every split / class size (running it, so writing
- * the outputs, a few times) and keep the fastest. */
+ * captured in a CUDA graph.  Requests of at least opts->conv_classes complex
+ * points run as class pipelines: the requests of one size, method and
+ * zero-pad setting go through five ordinary batched launches (the four-step
+ * phases) on parallel branches of the batch's graph.  The rest run longest
+ * first in a persistent kernel, whole in one CTA each or -- from
+ * opts->conv_split points -- as phase tasks spread over many CTAs.  flags: 0,
+ * or MUFFT_GB_FLAG_AUTOTUNE to time the batch with every split / class size
+ * (running it, so writing the outputs, a few times) and keep the fastest.
+ * opts: NULL for the defaults (mufft_gb_options_init). */
 mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *requests, unsigned count,
-                                                unsigned flags);
-/* Default split size of batches created afterwards: a power of two in
- * 16384..65536 complex points, or 0 to run every request whole. */
-int mufft_gb_set_conv_split(unsigned points);
-/* Requests of at least this many complex points (16384..65536, default
- * 16384; 0: none) in batches created afterwards run as class pipelines: the requests
- * of one size, method and zero-pad setting go through five ordinary batched
- * launches (the four-step phases), on parallel branches of the batch's graph,
- * beside the persistent kernel that runs the rest. */
-int mufft_gb_set_conv_classes(unsigned points);
+                                                unsigned flags, const mufft_gb_options *opts);
 /* The split size in use (complex points; 0: no request is split). */
 unsigned mufft_gb_conv_batch_split_size(const mufft_gb_conv_batch *batch);
 /* The class-pipeline size in use (complex points; 0: none). */
@@ -208,8 +275,17 @@ void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch);
  *   filter: `taps` floats in host or device memory (copied here).
  * No counterpart in the reference. */
 typedef struct mufft_gb_stream_conv mufft_gb_stream_conv;
+/* opts: NULL for the defaults.  opts->stream_conv_ranges: partition ranges
+ * the multiply-accumulate splits the P partitions into (each range a row of
+ * CTAs whose partial sums are added in range order; 0 sizes it to the GPU;
+ * clamped to P, or P - 1 for one-launch blocks, which also keep every CTA
+ * resident at once).  opts->stream_conv_fused: convolvers whose windows one
+ * 256-thread row tile transforms (64 .. 4096 complex points) run a block as
+ * one launch -- the forward transform, the multiply-accumulate and the
+ * inverse transform in one grid, ordered by tickets (1) -- or as a graph of
+ * separate launches (0). */
 mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned method, const float *filter, unsigned taps,
-                                                  unsigned flags);
+                                                  unsigned flags, const mufft_gb_options *opts);
 /* Device buffer the next input block goes into (block floats or complex).
  * Write it on the stream that runs mufft_gb_stream_conv_process, after the
  * previous process call. */
@@ -221,20 +297,9 @@ int mufft_gb_stream_conv_process(mufft_gb_stream_conv *conv, void *stream);
 /* Forgets the input history (as if the stream restarted from silence). */
 int mufft_gb_stream_conv_reset(mufft_gb_stream_conv *conv, void *stream);
 void mufft_gb_free_stream_conv(mufft_gb_stream_conv *conv);
-/* Partition ranges the multiply-accumulate of convolvers created afterwards
- * splits the P partitions into (each range a row of CTAs whose partial sums
- * are added in range order); 0, the default, sizes it to the GPU.  Values
- * are clamped to the partitions (P, or P - 1 for one-launch blocks, which
- * also keep every CTA resident at once). */
-int mufft_gb_set_stream_conv_ranges(unsigned ranges);
-/* Partition ranges a convolver uses. */
+/* Partition ranges a convolver uses, and whether it runs a block as one
+ * launch (1) or a graph of launches (0). */
 unsigned mufft_gb_stream_conv_ranges(const mufft_gb_stream_conv *conv);
-/* Convolvers created afterwards whose windows one 256-thread row tile
- * transforms (64 .. 4096 complex points) run a block as one launch -- the
- * forward transform, the multiply-accumulate and the inverse transform in
- * one grid, ordered by tickets (1, default) -- or as a graph of separate
- * launches (0).  mufft_gb_stream_conv_fused reports which a convolver uses. */
-int mufft_gb_set_stream_conv_fused(int enable);
 int mufft_gb_stream_conv_fused(const mufft_gb_stream_conv *conv);
 /* Synchronises the device; MUFFT_GB_ERR_UNSUPPORTED if a one-launch block's
  * bounded wait timed out since the last call (clearing the flag).  The
@@ -283,32 +348,12 @@ int mufft_gb_plan_1d_describe(const mufft_plan_1d *plan, char *buf, size_t size)
 int mufft_gb_plan_2d_describe(const mufft_plan_2d *plan, char *buf, size_t size);
 
 /* The same description for a 1D plan that would be built from these
- * arguments, computed on the host without touching a GPU (kind: 0 c2c,
- * 1 r2c, 2 c2r).  Returns MUFFT_GB_OK or the error plan creation would
- * report. */
+ * arguments and options, computed on the host without touching a GPU (kind:
+ * 0 c2c, 1 r2c, 2 c2r).  Returns MUFFT_GB_OK or the error plan creation
+ * would report. */
 int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned flags, unsigned batch,
-                                  char *buf, size_t size);
+                                  const mufft_gb_options *opts, char *buf, size_t size);
 
-/* ----------------------------------------------------------- tuning */
-
-/* Process-wide choice of the tile kernel used for transforms of length L
- * whose loads / stores walk across neighbouring transforms (nonzero) or
- * along one transform (zero): transforms_per_tile, elems_per_thread and
- * cluster_ctas (CTAs a tile is spread over) select among the compiled
- * variants (mufft_gb_list_tiles; 0 = any); all three 0 restores the default.
- * Affects plans created afterwards. */
-int mufft_gb_set_tile_choice(unsigned L, int load_across, int store_across, unsigned transforms_per_tile,
-                             unsigned elems_per_thread, unsigned cluster_ctas);
-/* Passes used for transforms longer than one on-chip tile (16384 points):
- * 2 (four-step) or 3 (three-level decomposition with smaller tiles); 0
- * restores the automatic choice.  Affects plans created afterwards. */
-int mufft_gb_set_multipass_levels(unsigned levels);
-/* Inter-pass twiddles of multi-pass transforms: from sincospif per element
- * (0), from a per-plan FP64 table times a per-tile factor (1), or from
- * per-tile column powers times one factor per thread (2); -1 restores the
- * automatic choice (2 where the column tile has room, else 0).  Affects plans
- * created afterwards. */
-int mufft_gb_set_twiddle_table(int mode);
 /* --------------------------------------------------------- autotuning */
 
 /* Times the candidate GPU schedules of a 1D plan shape (kind 0 c2c, 1 r2c,
@@ -326,32 +371,6 @@ int mufft_gb_autotune_save(const char *path);
 int mufft_gb_autotune_load(const char *path);
 void mufft_gb_autotune_clear(void);
 
-/* Columns of 2D plans created afterwards: 0 automatic (columns of 8192 points
- * and more as a two-pass four-step of short, wide column tiles), 1 one pass of
- * whole-column tiles, 2 the two-pass form whenever the column length allows. */
-int mufft_gb_set_2d_columns(int mode);
-/* Column passes of multi-pass plans created afterwards stage each tile
- * through a TMA tensor copy into shared memory, double-buffered in
- * persistent CTAs (1) or single-buffered (2), or load it with per-thread
- * loads (0, default). */
-int mufft_gb_set_tma(int mode);
-/* Tile passes of plans created afterwards run at most `ctas_per_sm` CTAs per
- * SM (they request the matching share of shared memory); 0, the default, lets
- * as many run as fit.  A grid that fills the GPU about once then runs in
- * several waves, and CTAs loading their inputs overlap CTAs storing results. */
-int mufft_gb_set_tile_occupancy(int ctas_per_sm);
-/* Contiguous row passes (batched 1D transforms, 2D rows) of plans created
- * afterwards run as persistent CTAs that prefetch their next tile's inputs
- * while they transform the current one (1), or as one CTA per tile (0). */
-int mufft_gb_set_stream_tiles(int enable);
-/* Split-precision plans (MUFFT_GB_FLAG_SPLIT_*) created afterwards run their
- * products on tcgen05.mma with TMEM accumulators (0, default) or on
- * warp-level mma.sync (1). */
-int mufft_gb_set_split_engine(int engine);
-/* Three-level transforms of N1 x 65536 points run their last two passes as one
- * persistent launch whose intermediate stays in L2 (enable = 1) or as two
- * launches (0, default).  Affects plans created afterwards. */
-int mufft_gb_set_fused_passes(int enable);
 /* Writes "L=.. R=.. C=.. Q=.. along/across threads=.. smem=..; ..." for every
  * compiled tile kernel; returns the full length. */
 int mufft_gb_list_tiles(char *buf, size_t size);

@@ -82,45 +82,36 @@ GB_H = [
     ("execute_plan_2d_launches_async", _i, [_vp, _vp, _vp, _u, _u, _vp]),
     ("plan_1d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("plan_2d_describe", _i, [_vp, C.c_char_p, _sz]),
-    ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, C.c_char_p, _sz]),
-    ("set_tile_choice", _i, [_u, _i, _i, _u, _u, _u]),
-    ("set_multipass_levels", _i, [_u]),
-    ("set_twiddle_table", _i, [_i]),
-    ("set_fused_passes", _i, [_i]),
+    ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, _vp, C.c_char_p, _sz]),
+    ("options_init", None, [_vp]),
+    ("create_plan_1d", _vp, [_i, _u, _i, _u, _u, _sz, _sz, _vp]),
+    ("create_plan_2d", _vp, [_i, _u, _u, _i, _u, _vp]),
+    ("create_plan_conv", _vp, [_u, _u, _u, _vp]),
     ("list_tiles", _i, [C.c_char_p, _sz]),
     ("execute_c2c_noalloc", _i, [_u, _i, _vp, _vp, _vp]),
     ("conv_adjoint_input", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("conv_adjoint_filter", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _u, _vp]),
     ("conv_adjoint", _i, [_vp, _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _u, _vp]),
     ("execute_conv_output_batched", _i, [_vp, _vp, _sz, _vp, _sz, _vp, _u, _vp]),
-    ("set_split_engine", _i, [_i]),
-    ("set_tma", _i, [_i]),
-    ("set_tile_occupancy", _i, [_i]),
-    ("set_stream_tiles", _i, [_i]),
-    ("set_2d_columns", _i, [_i]),
     ("autotune_1d", _i, [_i, _u, _i, _u, _u, _vp, _sz]),
     ("autotune_save", _i, [C.c_char_p]),
     ("autotune_load", _i, [C.c_char_p]),
     ("autotune_clear", None, []),
-    ("create_stream_conv", _vp, [_u, _u, _vp, _u, _u]),
+    ("create_stream_conv", _vp, [_u, _u, _vp, _u, _u, _vp]),
     ("stream_conv_input", _vp, [_vp]),
     ("stream_conv_output", _vp, [_vp]),
     ("stream_conv_process", _i, [_vp, _vp]),
     ("stream_conv_reset", _i, [_vp, _vp]),
-    ("set_stream_conv_ranges", _i, [_u]),
     ("stream_conv_ranges", _u, [_vp]),
-    ("set_stream_conv_fused", _i, [_i]),
     ("stream_conv_fused", _i, [_vp]),
     ("stream_conv_status", _i, [_vp]),
     ("stream_conv_inject_timeout", _i, [_vp, _i]),
     ("free_stream_conv", None, [_vp]),
-    ("create_conv_batch", _vp, [_vp, _u, _u]),
+    ("create_conv_batch", _vp, [_vp, _u, _u, _vp]),
     ("execute_conv_batch", _i, [_vp, _vp]),
     ("conv_batch_split_size", _u, [_vp]),
     ("conv_batch_class_size", _u, [_vp]),
     ("conv_batch_status", _i, [_vp]),
-    ("set_conv_split", _i, [_u]),
-    ("set_conv_classes", _i, [_u]),
     ("free_conv_batch", None, [_vp]),
     ("device_alloc", _vp, [_sz]),
     ("device_free", None, [_vp]),
@@ -135,6 +126,24 @@ class ConvRequest(C.Structure):
     """mufft_gb_conv_request (include/mufft_gb300.h)."""
     _fields_ = [("N", C.c_uint), ("method", C.c_uint), ("input", C.c_void_p), ("filter", C.c_void_p),
                 ("output", C.c_void_p)]
+
+
+class TileChoice(C.Structure):
+    """mufft_gb_tile_choice (include/mufft_gb300.h)."""
+    _fields_ = [("L", C.c_uint), ("load_across", C.c_int), ("store_across", C.c_int),
+                ("transforms_per_tile", C.c_uint), ("elems_per_thread", C.c_uint), ("cluster_ctas", C.c_uint)]
+
+
+MAX_TILE_CHOICES = 8
+
+
+class Options(C.Structure):
+    """mufft_gb_options (include/mufft_gb300.h): per-plan schedule choices."""
+    _fields_ = [("size", C.c_uint), ("multipass_levels", C.c_int), ("twiddle_table", C.c_int),
+                ("fused_passes", C.c_int), ("tma", C.c_int), ("tile_occupancy", C.c_int), ("stream_tiles", C.c_int),
+                ("split_engine", C.c_int), ("columns_2d", C.c_int), ("conv_split", C.c_uint),
+                ("conv_classes", C.c_uint), ("stream_conv_ranges", C.c_uint), ("stream_conv_fused", C.c_int),
+                ("ntiles", C.c_uint), ("tiles", TileChoice * MAX_TILE_CHOICES)]
 
 
 class MuFFTError(RuntimeError):
@@ -197,6 +206,22 @@ class MuFFT:
         f.argtypes = args
         setattr(self, pyname, f)
         self.symbols.append(cname)
+
+    # ---------------------------------------------------------- options
+    def options(self, tiles=(), **fields) -> "Options":
+        """mufft_gb_options with the library's defaults, then `fields` set
+        (names as in the C struct); `tiles`: (L, load_across, store_across,
+        transforms_per_tile, elems_per_thread, cluster_ctas) tuples."""
+        o = Options()
+        self.gb_options_init(C.byref(o))
+        for k, v in fields.items():
+            if not hasattr(o, k) or k in ("size", "tiles", "ntiles"):
+                raise AttributeError(f"no option {k}")
+            setattr(o, k, v)
+        for i, t in enumerate(tiles):
+            o.tiles[i] = TileChoice(*t)
+        o.ntiles = len(tiles)
+        return o
 
     # ----------------------------------------------------------- errors
     def check(self, what: str = "call"):
@@ -271,10 +296,21 @@ class MuFFT:
             self.free_plan_conv(plan)
         return out
 
-    def fft2_c2c(self, x: np.ndarray, direction: int, flags: int = 0) -> np.ndarray:
+    def _plan_2d(self, kind: int, Nx: int, Ny: int, direction: int, flags: int, opts):
+        if opts is not None:
+            return self._plan(self.gb_create_plan_2d(kind, Nx, Ny, direction, flags, C.byref(opts)),
+                              "gb_create_plan_2d")
+        if kind == 0:
+            return self._plan(self.create_plan_2d_c2c(Nx, Ny, direction, flags), "create_plan_2d_c2c")
+        if kind == 1:
+            return self._plan(self.create_plan_2d_r2c(Nx, Ny, flags), "create_plan_2d_r2c")
+        return self._plan(self.create_plan_2d_c2r(Nx, Ny, flags), "create_plan_2d_c2r")
+
+    def fft2_c2c(self, x: np.ndarray, direction: int, flags: int = 0, opts=None) -> np.ndarray:
+        """opts: mufft_gb_options for the GB300 library (None: the fft.h creator)."""
         x = aligned_copy(x, np.complex64)
         Ny, Nx = x.shape
-        plan = self._plan(self.create_plan_2d_c2c(Nx, Ny, direction, flags), "create_plan_2d_c2c")
+        plan = self._plan_2d(0, Nx, Ny, direction, flags, opts)
         out = aligned_zeros((Ny, Nx), np.complex64)
         try:
             self.execute_plan_2d(plan, _ptr(out), _ptr(x))
@@ -283,11 +319,11 @@ class MuFFT:
             self.free_plan_2d(plan)
         return out
 
-    def fft2_r2c(self, x: np.ndarray, flags: int = 0) -> np.ndarray:
+    def fft2_r2c(self, x: np.ndarray, flags: int = 0, opts=None) -> np.ndarray:
         """Returns the Ny x Nx complex output buffer (valid columns Nx/2 + 1, or Nx with FULL_R2C)."""
         x = aligned_copy(x, np.float32)
         Ny, Nx = x.shape
-        plan = self._plan(self.create_plan_2d_r2c(Nx, Ny, flags), "create_plan_2d_r2c")
+        plan = self._plan_2d(1, Nx, Ny, FORWARD, flags, opts)
         out = aligned_zeros((Ny, Nx), np.complex64)
         try:
             self.execute_plan_2d(plan, _ptr(out), _ptr(x))
@@ -296,11 +332,11 @@ class MuFFT:
             self.free_plan_2d(plan)
         return out
 
-    def fft2_c2r(self, X: np.ndarray, flags: int = 0) -> np.ndarray:
+    def fft2_c2r(self, X: np.ndarray, flags: int = 0, opts=None) -> np.ndarray:
         """X: Ny x Nx complex buffer (first Nx/2 + 1 columns read); returns Ny x Nx reals."""
         X = aligned_copy(X, np.complex64)
         Ny, Nx = X.shape
-        plan = self._plan(self.create_plan_2d_c2r(Nx, Ny, flags), "create_plan_2d_c2r")
+        plan = self._plan_2d(2, Nx, Ny, INVERSE, flags, opts)
         out = aligned_zeros(2 * Nx * Ny, np.float32)  # the reference's scratch contract (fft.h:258-260)
         try:
             self.execute_plan_2d(plan, _ptr(out), _ptr(X))

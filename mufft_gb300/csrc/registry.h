@@ -27,9 +27,8 @@ void register_tiles_transpose(std::vector<TileKernel> &out);
 
 // Returns the instantiation for (L, lmap, smap): the one matching the
 // nonzero of C (transforms per tile), R (elements per thread) and Q (cluster
-// size), else the preferred one (set_tile_choice) or the first registered.
-// nullptr if none exists.
+// size), else the one the options of the plan being built prefer, else the
+// first registered.  nullptr if none exists.
 const TileKernel *find_tile(int L, int lmap, int smap, int C = 0, int R = 0, int Q = 0);
-bool set_tile_choice(int L, int lmap, int smap, int C, int R = 0, int Q = 0);
 
 }  // namespace mgb

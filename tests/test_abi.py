@@ -83,24 +83,22 @@ def test_extension_flags_match_header():
 
 def test_split_precision_schedule_and_rejections(lib):
     buf = C.create_string_buffer(4096)
-    try:
-        for N, limbs, flag in ((4096, 3, K.FLAG_SPLIT_BF16X3), (256, 2, K.FLAG_SPLIT_BF16X2)):
-            assert lib.gb_set_split_engine(1) == 0  # mma.sync: one CTA per 4096 points
-            assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, buf, 4096) == 0
-            d = buf.value.decode()
-            assert d.startswith(f"split_tc N={N} bf16x{limbs} mma.sync"), d
-            assert f"grid={65536 * N // 4096}" in d, d
-            assert lib.gb_set_split_engine(0) == 0  # tcgen05: persistent, two CTAs per SM
-            assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, buf, 4096) == 0
-            d = buf.value.decode()
-            assert d.startswith(f"split_tc N={N} bf16x{limbs} tcgen05 grid=304"), d
-    finally:
-        lib.gb_set_split_engine(0)
-    assert lib.gb_set_split_engine(2) == -1
+    for N, limbs, flag in ((4096, 3, K.FLAG_SPLIT_BF16X3), (256, 2, K.FLAG_SPLIT_BF16X2)):
+        mma_sync = lib.options(split_engine=1)  # one CTA per 4096 points
+        assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, C.byref(mma_sync), buf, 4096) == 0
+        d = buf.value.decode()
+        assert d.startswith(f"split_tc N={N} bf16x{limbs} mma.sync"), d
+        assert f"grid={65536 * N // 4096}" in d, d
+        # tcgen05 (the default): persistent, two CTAs per SM
+        assert lib.gb_describe_schedule_1d(N, 0, K.FORWARD, flag, 65536, None, buf, 4096) == 0
+        d = buf.value.decode()
+        assert d.startswith(f"split_tc N={N} bf16x{limbs} tcgen05 grid=304"), d
+    bad = lib.options(split_engine=2)
+    assert lib.gb_describe_schedule_1d(4096, 0, K.FORWARD, K.FLAG_SPLIT_BF16X3, 1, C.byref(bad), buf, 4096) == -1
     lib.gb_clear_error()
     for N, kind, flags in ((1024, 0, K.FLAG_SPLIT_BF16X3), (4096, 1, K.FLAG_SPLIT_BF16X3),
                            (4096, 0, K.FLAG_SPLIT_BF16X2 | K.FLAG_ZERO_PAD_UPPER_HALF)):
-        assert lib.gb_describe_schedule_1d(N, kind, K.FORWARD, flags, 1, buf, 4096) == -2, (N, kind, flags)
+        assert lib.gb_describe_schedule_1d(N, kind, K.FORWARD, flags, 1, None, buf, 4096) == -2, (N, kind, flags)
         lib.gb_clear_error()
 
 
@@ -129,7 +127,7 @@ def test_stream_conv_validates_on_host(lib):
     import numpy as np
     h = np.ones(10, np.float32)
     for block, taps in ((1000, 10), (1, 10), (256, 0)):
-        assert not lib.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0)
+        assert not lib.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0, None)
         assert lib.gb_last_error() == -1
         lib.gb_clear_error()
     assert not lib.gb_stream_conv_input(None) and not lib.gb_stream_conv_output(None)
@@ -183,18 +181,18 @@ def test_conv_batch_validates_requests_on_host(lib):
              (1024, 0, (fake, None, fake), -1)]
     for N, method, ptrs, code in cases:
         reqs = (K.ConvRequest * 1)(K.ConvRequest(N, method, *ptrs))
-        assert not lib.gb_create_conv_batch(reqs, 1, 0)
+        assert not lib.gb_create_conv_batch(reqs, 1, 0, None)
         assert lib.gb_last_error() == code, (N, method)
         lib.gb_clear_error()
-    assert not lib.gb_create_conv_batch(None, 0, 0)
+    assert not lib.gb_create_conv_batch(None, 0, 0, None)
     assert lib.gb_last_error() == -1
     lib.gb_clear_error()
     lib.gb_free_conv_batch(None)
 
 
-def _sched(lib, N, kind, direction=K.FORWARD, flags=0, batch=1):
+def _sched(lib, N, kind, direction=K.FORWARD, flags=0, batch=1, opts=None):
     buf = C.create_string_buffer(4096)
-    rc = lib.gb_describe_schedule_1d(N, kind, direction, flags, batch, buf, 4096)
+    rc = lib.gb_describe_schedule_1d(N, kind, direction, flags, batch, C.byref(opts) if opts else None, buf, 4096)
     assert rc == 0, (rc, lib.gb_last_error_string())
     return buf.value.decode()
 
@@ -211,28 +209,22 @@ def test_single_pass_schedule(lib):
 
 
 def test_multipass_schedules(lib):
-    try:
-        assert lib.gb_set_multipass_levels(2) == 0
-        parts = _sched(lib, 1 << 24, 0).split("; ")
-        assert len(parts) == 2
-        assert "L=4096" in parts[0] and "across/across" in parts[0] and "epi=twiddle" in parts[0]
-        assert "L=4096" in parts[1] and "along/across" in parts[1]
-        assert lib.gb_set_multipass_levels(3) == 0
-        assert lib.gb_set_fused_passes(0) == 0
-        parts = _sched(lib, 1 << 24, 0).split("; ")
-        assert len(parts) == 3
-        assert all("L=256" in p for p in parts)
-        assert "epi=twiddle" in parts[0] and "epi=twiddle" in parts[1]
-        assert "along/across" in parts[2] and "grid=16x256" in parts[2]
-        assert lib.gb_set_fused_passes(1) == 0
-        parts = _sched(lib, 1 << 24, 0).split("; ")
-        assert len(parts) == 2 and "L=256" in parts[0] and parts[1].startswith("fused_bc")
-        assert "blocks=16 ring=4" in parts[1]
-        assert lib.gb_set_multipass_levels(5) == -1
-        lib.gb_clear_error()
-    finally:
-        lib.gb_set_multipass_levels(0)
-        lib.gb_set_fused_passes(0)
+    parts = _sched(lib, 1 << 24, 0, opts=lib.options(multipass_levels=2)).split("; ")
+    assert len(parts) == 2
+    assert "L=4096" in parts[0] and "across/across" in parts[0] and "epi=twiddle" in parts[0]
+    assert "L=4096" in parts[1] and "along/across" in parts[1]
+    parts = _sched(lib, 1 << 24, 0, opts=lib.options(multipass_levels=3, fused_passes=0)).split("; ")
+    assert len(parts) == 3
+    assert all("L=256" in p for p in parts)
+    assert "epi=twiddle" in parts[0] and "epi=twiddle" in parts[1]
+    assert "along/across" in parts[2] and "grid=16x256" in parts[2]
+    parts = _sched(lib, 1 << 24, 0, opts=lib.options(multipass_levels=3, fused_passes=1)).split("; ")
+    assert len(parts) == 2 and "L=256" in parts[0] and parts[1].startswith("fused_bc")
+    assert "blocks=16 ring=4" in parts[1]
+    buf = C.create_string_buffer(64)
+    bad = lib.options(multipass_levels=5)
+    assert lib.gb_describe_schedule_1d(1 << 24, 0, K.FORWARD, 0, 1, C.byref(bad), buf, 64) == -1
+    lib.gb_clear_error()
     s = _sched(lib, 1 << 21, 1)  # r2c of 2^21 reals = 2^20 complex + in-place fix-up
     assert s.split("; ")[-1].startswith("r2c_fixup")
 
@@ -240,25 +232,32 @@ def test_multipass_schedules(lib):
 def test_schedule_options_in_dry_runs(lib):
     """Resident-CTA caps pad the tile launches' shared memory; streaming row
     tiles run as a persistent grid (both measured slower on GB300, off by
-    default); the defaults are restored."""
-    try:
-        assert lib.gb_set_tile_occupancy(2) == 0
-        s = _sched(lib, 1024, 0, batch=4096)
-        assert "smem=115712" in s, s          # (233472 / 2 - 1024) rounded to 128 bytes
-        assert lib.gb_set_tile_occupancy(0) == 0
-        assert lib.gb_set_stream_tiles(1) == 0
-        s = _sched(lib, 1024, 0, batch=4096)
-        assert "tile+stream" in s and "grid=152x1" in s, s
-    finally:
-        lib.gb_set_tile_occupancy(0)
-        lib.gb_set_stream_tiles(0)
+    default); options apply to the one call they are passed to."""
+    s = _sched(lib, 1024, 0, batch=4096, opts=lib.options(tile_occupancy=2))
+    assert "smem=115712" in s, s          # (233472 / 2 - 1024) rounded to 128 bytes
+    s = _sched(lib, 1024, 0, batch=4096, opts=lib.options(stream_tiles=1))
+    assert "tile+stream" in s and "grid=152x1" in s, s
     s = _sched(lib, 1024, 0, batch=4096)
     assert "+stream" not in s and "smem=34816" in s
-    for bad in (lambda: lib.gb_set_tile_occupancy(-1), lambda: lib.gb_set_tile_occupancy(33),
-                lambda: lib.gb_set_stream_tiles(2), lambda: lib.gb_set_stream_conv_fused(3),
-                lambda: lib.gb_set_stream_conv_ranges(1 << 21)):
-        assert bad() == -1
+    s = _sched(lib, 1024, 0, batch=4096, opts=lib.options(tiles=[(1024, 0, 0, 1, 16, 1)]))
+    assert "L=1024 R=16 C=1 " in s and "grid=4096x1" in s, s
+    buf = C.create_string_buffer(64)
+    for bad in (dict(tile_occupancy=-1), dict(tile_occupancy=33), dict(stream_tiles=2), dict(stream_conv_fused=3),
+                dict(stream_conv_ranges=1 << 21), dict(conv_split=1000), dict(twiddle_table=3), dict(tma=3),
+                dict(columns_2d=3)):
+        o = lib.options(**bad)
+        assert lib.gb_describe_schedule_1d(1024, 0, K.FORWARD, 0, 1, C.byref(o), buf, 64) == -1, bad
         lib.gb_clear_error()
+    o = lib.options(tiles=[(1024, 0, 0, 3, 0, 0)])  # no such tile
+    assert lib.gb_describe_schedule_1d(1024, 0, K.FORWARD, 0, 1, C.byref(o), buf, 64) == -1
+    lib.gb_clear_error()
+    o = lib.options()
+    o.size = 4  # not initialised by mufft_gb_options_init
+    assert lib.gb_describe_schedule_1d(1024, 0, K.FORWARD, 0, 1, C.byref(o), buf, 64) == -1
+    lib.gb_clear_error()
+    d = lib.options()
+    assert (d.multipass_levels, d.twiddle_table, d.conv_split, d.conv_classes, d.stream_conv_fused) == \
+        (0, -1, 65536, 16384, 1)
 
 
 def test_batched_convolution_entry_points_validate_on_host(lib):

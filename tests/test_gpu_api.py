@@ -172,26 +172,19 @@ def test_multipass_variants(gpu, torch, levels, fused, table, N, B):
     x = signals.complex_uniform(25000 + N + B, N * B).reshape(B, N)
     dx = _dev(torch, x)
     dy = torch.empty_like(dx)
-    try:
-        assert gpu.gb_set_multipass_levels(levels) == 0
-        assert gpu.gb_set_fused_passes(fused) == 0
-        assert gpu.gb_set_twiddle_table(table) == 0
-        for direction in (K.FORWARD, K.INVERSE):
-            plan = gpu.gb_create_plan_1d_c2c_batched(N, direction, 0, B, 0, 0)
-            assert plan, gpu.gb_last_error_string()
-            assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
-            torch.cuda.synchronize()
-            gpu.free_plan_1d(plan)
-            got = dy.cpu().numpy()
-            for r in range(B):
-                ref = np.fft.fft(x[r].astype(np.complex128))
-                if direction == K.INVERSE:
-                    ref = np.fft.ifft(x[r].astype(np.complex128)) * N
-                assert rel_l2(got[r], ref) < 2e-6, (r, direction)
-    finally:
-        gpu.gb_set_multipass_levels(0)
-        gpu.gb_set_fused_passes(0)
-        gpu.gb_set_twiddle_table(-1)
+    opts = gpu.options(multipass_levels=levels, fused_passes=fused, twiddle_table=table)
+    for direction in (K.FORWARD, K.INVERSE):
+        plan = gpu.gb_create_plan_1d(0, N, direction, 0, B, 0, 0, C.byref(opts))
+        assert plan, gpu.gb_last_error_string()
+        assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
+        torch.cuda.synchronize()
+        gpu.free_plan_1d(plan)
+        got = dy.cpu().numpy()
+        for r in range(B):
+            ref = np.fft.fft(x[r].astype(np.complex128))
+            if direction == K.INVERSE:
+                ref = np.fft.ifft(x[r].astype(np.complex128)) * N
+            assert rel_l2(got[r], ref) < 2e-6, (r, direction)
 
 
 @pytest.mark.parametrize("mode", [1, 2])
@@ -202,25 +195,22 @@ def test_tma_staged_column_passes(gpu, torch, mode, N, B):
     x = signals.complex_uniform(26000 + N + B, N * B).reshape(B, N)
     dx = _dev(torch, x)
     dy = torch.empty_like(dx)
-    try:
-        assert gpu.gb_set_tma(mode) == 0
-        for direction in (K.FORWARD, K.INVERSE):
-            plan = gpu.gb_create_plan_1d_c2c_batched(N, direction, 0, B, 0, 0)
-            assert plan, gpu.gb_last_error_string()
-            buf = C.create_string_buffer(4096)
-            gpu.gb_plan_1d_describe(plan, buf, 4096)
-            assert b"+tma" in buf.value, buf.value
-            assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
-            torch.cuda.synchronize()
-            gpu.free_plan_1d(plan)
-            got = dy.cpu().numpy()
-            for r in range(B):
-                ref = np.fft.fft(x[r].astype(np.complex128))
-                if direction == K.INVERSE:
-                    ref = np.fft.ifft(x[r].astype(np.complex128)) * N
-                assert rel_l2(got[r], ref) < 2e-6, (r, direction)
-    finally:
-        gpu.gb_set_tma(0)
+    opts = gpu.options(tma=mode)
+    for direction in (K.FORWARD, K.INVERSE):
+        plan = gpu.gb_create_plan_1d(0, N, direction, 0, B, 0, 0, C.byref(opts))
+        assert plan, gpu.gb_last_error_string()
+        buf = C.create_string_buffer(4096)
+        gpu.gb_plan_1d_describe(plan, buf, 4096)
+        assert b"+tma" in buf.value, buf.value
+        assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
+        torch.cuda.synchronize()
+        gpu.free_plan_1d(plan)
+        got = dy.cpu().numpy()
+        for r in range(B):
+            ref = np.fft.fft(x[r].astype(np.complex128))
+            if direction == K.INVERSE:
+                ref = np.fft.ifft(x[r].astype(np.complex128)) * N
+            assert rel_l2(got[r], ref) < 2e-6, (r, direction)
 
 
 @pytest.mark.parametrize("N,B", [(256, 1000), (1024, 4096), (2048, 333), (4096, 77)])
@@ -230,40 +220,37 @@ def test_streamed_row_tiles(gpu, torch, N, B):
     x = signals.complex_uniform(27000 + N + B, N * B).reshape(B, N)
     xr = signals.uniform(27500 + N + B, N * B).reshape(B, N)
     st = _stream(torch)
-    try:
-        assert gpu.gb_set_stream_tiles(1) == 0
-        dx = _dev(torch, x)
-        dy = torch.empty_like(dx)
-        for direction in (K.FORWARD, K.INVERSE):
-            plan = gpu.gb_create_plan_1d_c2c_batched(N, direction, 0, B, 0, 0)
-            assert plan, gpu.gb_last_error_string()
-            buf = C.create_string_buffer(4096)
-            gpu.gb_plan_1d_describe(plan, buf, 4096)
-            assert b"+stream" in buf.value, buf.value
-            assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), st) == 0
-            torch.cuda.synchronize()
-            gpu.free_plan_1d(plan)
-            got = dy.cpu().numpy()
-            ref = np.fft.fft(x.astype(np.complex128), axis=1) if direction == K.FORWARD else \
-                np.fft.ifft(x.astype(np.complex128), axis=1) * N
-            assert rel_l2(got, ref) < 2e-6, direction
-        M = N // 2 + 1
-        dxr = _dev(torch, xr)
-        dX = torch.empty(B * M, dtype=torch.complex64, device="cuda")
-        dyr = torch.empty(B * N, dtype=torch.float32, device="cuda")
-        pf = gpu.gb_create_plan_1d_r2c_batched(N, 0, B, 0, 0)
-        pb = gpu.gb_create_plan_1d_c2r_batched(N, 0, B, 0, 0)
-        assert pf and pb, gpu.gb_last_error_string()
-        assert gpu.gb_execute_plan_1d_async(pf, dX.data_ptr(), dxr.data_ptr(), st) == 0
-        assert gpu.gb_execute_plan_1d_async(pb, dyr.data_ptr(), dX.data_ptr(), st) == 0
+    opts = gpu.options(stream_tiles=1)
+    dx = _dev(torch, x)
+    dy = torch.empty_like(dx)
+    for direction in (K.FORWARD, K.INVERSE):
+        plan = gpu.gb_create_plan_1d(0, N, direction, 0, B, 0, 0, C.byref(opts))
+        assert plan, gpu.gb_last_error_string()
+        buf = C.create_string_buffer(4096)
+        gpu.gb_plan_1d_describe(plan, buf, 4096)
+        assert b"+stream" in buf.value, buf.value
+        assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), st) == 0
         torch.cuda.synchronize()
-        gpu.free_plan_1d(pf)
-        gpu.free_plan_1d(pb)
-        ref = np.fft.rfft(xr.astype(np.float64), axis=1)
-        assert rel_l2(dX.cpu().numpy().reshape(B, M), ref) < 2e-6
-        assert rel_l2(dyr.cpu().numpy().reshape(B, N) / N, xr) < 2e-6
-    finally:
-        gpu.gb_set_stream_tiles(0)
+        gpu.free_plan_1d(plan)
+        got = dy.cpu().numpy()
+        ref = np.fft.fft(x.astype(np.complex128), axis=1) if direction == K.FORWARD else \
+            np.fft.ifft(x.astype(np.complex128), axis=1) * N
+        assert rel_l2(got, ref) < 2e-6, direction
+    M = N // 2 + 1
+    dxr = _dev(torch, xr)
+    dX = torch.empty(B * M, dtype=torch.complex64, device="cuda")
+    dyr = torch.empty(B * N, dtype=torch.float32, device="cuda")
+    pf = gpu.gb_create_plan_1d(1, N, K.FORWARD, 0, B, 0, 0, C.byref(opts))
+    pb = gpu.gb_create_plan_1d(2, N, K.INVERSE, 0, B, 0, 0, C.byref(opts))
+    assert pf and pb, gpu.gb_last_error_string()
+    assert gpu.gb_execute_plan_1d_async(pf, dX.data_ptr(), dxr.data_ptr(), st) == 0
+    assert gpu.gb_execute_plan_1d_async(pb, dyr.data_ptr(), dX.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    gpu.free_plan_1d(pf)
+    gpu.free_plan_1d(pb)
+    ref = np.fft.rfft(xr.astype(np.float64), axis=1)
+    assert rel_l2(dX.cpu().numpy().reshape(B, M), ref) < 2e-6
+    assert rel_l2(dyr.cpu().numpy().reshape(B, N) / N, xr) < 2e-6
 
 
 @pytest.mark.parametrize("occ", [1, 3, 8])
@@ -271,32 +258,29 @@ def test_tile_occupancy_cap(gpu, torch, occ):
     """Capped resident CTAs per SM (padded shared memory) change nothing in
     the results: a batched single pass, a multi-pass transform and a 2D r2c."""
     st = _stream(torch)
-    try:
-        assert gpu.gb_set_tile_occupancy(occ) == 0
-        for N, B in [(1024, 512), (1 << 20, 1)]:
-            x = signals.complex_uniform(28000 + N + occ, N * B).reshape(B, N)
-            dx = _dev(torch, x)
-            dy = torch.empty_like(dx)
-            plan = gpu.gb_create_plan_1d_c2c_batched(N, K.FORWARD, 0, B, 0, 0)
-            assert plan, gpu.gb_last_error_string()
-            assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), st) == 0
-            torch.cuda.synchronize()
-            gpu.free_plan_1d(plan)
-            assert rel_l2(dy.cpu().numpy(), np.fft.fft(x.astype(np.complex128), axis=1)) < 2e-6, (N, B)
-        Nx, Ny = 512, 256
-        xr = signals.uniform(28100 + occ, Nx * Ny).reshape(Ny, Nx)
-        plan = gpu.create_plan_2d_r2c(Nx, Ny, 0)
+    opts = gpu.options(tile_occupancy=occ)
+    for N, B in [(1024, 512), (1 << 20, 1)]:
+        x = signals.complex_uniform(28000 + N + occ, N * B).reshape(B, N)
+        dx = _dev(torch, x)
+        dy = torch.empty_like(dx)
+        plan = gpu.gb_create_plan_1d(0, N, K.FORWARD, 0, B, 0, 0, C.byref(opts))
         assert plan, gpu.gb_last_error_string()
-        dxr = _dev(torch, xr)
-        dX = torch.empty(Ny * Nx, dtype=torch.complex64, device="cuda")
-        assert gpu.gb_execute_plan_2d_async(plan, dX.data_ptr(), dxr.data_ptr(), st) == 0
+        assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), st) == 0
         torch.cuda.synchronize()
-        gpu.free_plan_2d(plan)
-        got = dX.cpu().numpy().reshape(Ny, Nx)[:, : Nx // 2 + 1]
-        assert rel_l2(got, np.fft.rfft2(xr.astype(np.float64))) < 2e-6
-    finally:
-        gpu.gb_set_tile_occupancy(0)
-    assert gpu.gb_set_tile_occupancy(-1) != 0
-    gpu.gb_clear_error()
-    assert gpu.gb_set_stream_tiles(2) != 0
+        gpu.free_plan_1d(plan)
+        assert rel_l2(dy.cpu().numpy(), np.fft.fft(x.astype(np.complex128), axis=1)) < 2e-6, (N, B)
+    Nx, Ny = 512, 256
+    xr = signals.uniform(28100 + occ, Nx * Ny).reshape(Ny, Nx)
+    plan = gpu.gb_create_plan_2d(1, Nx, Ny, K.FORWARD, 0, C.byref(opts))
+    assert plan, gpu.gb_last_error_string()
+    dxr = _dev(torch, xr)
+    dX = torch.empty(Ny * Nx, dtype=torch.complex64, device="cuda")
+    assert gpu.gb_execute_plan_2d_async(plan, dX.data_ptr(), dxr.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    gpu.free_plan_2d(plan)
+    got = dX.cpu().numpy().reshape(Ny, Nx)[:, : Nx // 2 + 1]
+    assert rel_l2(got, np.fft.rfft2(xr.astype(np.float64))) < 2e-6
+    bad = gpu.options(tile_occupancy=-1)
+    assert not gpu.gb_create_plan_1d(0, 1024, K.FORWARD, 0, 1, 0, 0, C.byref(bad))
+    assert gpu.gb_last_error() == -1
     gpu.gb_clear_error()

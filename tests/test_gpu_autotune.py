@@ -32,7 +32,8 @@ def torch():
 
 def describe(gpu, N, kind=0, flags=0, batch=1):
     buf = C.create_string_buffer(4096)
-    assert gpu.gb_describe_schedule_1d(N, kind, K.FORWARD if kind != 2 else K.INVERSE, flags, batch, buf, 4096) == 0
+    assert gpu.gb_describe_schedule_1d(N, kind, K.FORWARD if kind != 2 else K.INVERSE, flags, batch, None, buf,
+                                       4096) == 0
     return buf.value.decode()
 
 

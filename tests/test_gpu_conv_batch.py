@@ -57,7 +57,7 @@ def filter_spectrum(gpu, b: np.ndarray, N: int, method: int) -> np.ndarray:
 class Batch:
     """Device buffers and the batch handle for a list of (N, method) requests."""
 
-    def __init__(self, gpu, torch, specs, seed, flags=0):
+    def __init__(self, gpu, torch, specs, seed, flags=0, opts=None):
         self.gpu, self.specs = gpu, specs
         self.a, self.b, self.din, self.dh, self.dout = [], [], [], [], []
         reqs = (K.ConvRequest * len(specs))()
@@ -71,7 +71,7 @@ class Batch:
             dout = torch.full((N,), float("nan"), dtype=torch.complex64 if stereo else torch.float32, device="cuda")
             reqs[i] = K.ConvRequest(N, method, din.data_ptr(), dh.data_ptr(), dout.data_ptr())
             self.a.append(a), self.b.append(b), self.din.append(din), self.dh.append(dh), self.dout.append(dout)
-        self.handle = gpu.gb_create_conv_batch(reqs, len(specs), flags)
+        self.handle = gpu.gb_create_conv_batch(reqs, len(specs), flags, C.byref(opts) if opts else None)
         assert self.handle, gpu.gb_last_error_string()
 
     def run(self, torch):
@@ -168,10 +168,10 @@ def test_conv_batch_rejects_bad_requests(gpu, torch):
     for N, method, ptrs in [(1000, 0, (p, p, p)), (1 << 18, 0, (p, p, p)), (16, 0, (p, p, p)),
                             (1 << 17, STEREO, (p, p, p)), (1024, 0, (p, None, p))]:
         reqs = (K.ConvRequest * 1)(K.ConvRequest(N, method, *ptrs))
-        assert not gpu.gb_create_conv_batch(reqs, 1, 0)
+        assert not gpu.gb_create_conv_batch(reqs, 1, 0, None)
         assert gpu.gb_last_error() in (-1, -2), (N, method)
         gpu.gb_clear_error()
-    assert not gpu.gb_create_conv_batch(None, 0, 0)
+    assert not gpu.gb_create_conv_batch(None, 0, 0, None)
     gpu.gb_clear_error()
 
 
@@ -199,13 +199,7 @@ def test_conv_batch_forced_split_sizes(gpu, ora, torch, split):
     bounded dependency waits, or whole requests)."""
     specs = [(1 << 17, 0), (1 << 16, STEREO), (1 << 15, PAD1), (1 << 15, STEREO | PAD1), (1 << 16, PAD1 | PAD2),
              (1 << 14, STEREO), (2048, 0), (64, STEREO)]
-    try:
-        assert gpu.gb_set_conv_split(split) == 0
-        assert gpu.gb_set_conv_classes(0) == 0
-        bt = Batch(gpu, torch, specs, 95000 + split)
-    finally:
-        gpu.gb_set_conv_split(1 << 16)
-        gpu.gb_set_conv_classes(1 << 14)
+    bt = Batch(gpu, torch, specs, 95000 + split, opts=gpu.options(conv_split=split, conv_classes=0))
     try:
         assert gpu.gb_conv_batch_split_size(bt.handle) == split
         outs = bt.run(torch)
@@ -221,11 +215,7 @@ def test_conv_batch_class_pipelines(gpu, ora, torch, classes):
     parallel graph branches) beside the persistent kernel."""
     specs = [(1 << 17, 0), (1 << 16, STEREO), (1 << 15, PAD1), (1 << 15, STEREO | PAD1), (1 << 16, PAD1 | PAD2),
              (1 << 14, STEREO), (1 << 17, PAD1), (1 << 16, STEREO), (2048, 0), (64, STEREO)]
-    try:
-        assert gpu.gb_set_conv_classes(classes) == 0
-        bt = Batch(gpu, torch, specs, 96000 + classes)
-    finally:
-        gpu.gb_set_conv_classes(1 << 14)
+    bt = Batch(gpu, torch, specs, 96000 + classes, opts=gpu.options(conv_classes=classes))
     try:
         assert gpu.gb_conv_batch_class_size(bt.handle) == classes
         outs = bt.run(torch)
@@ -280,7 +270,7 @@ def test_conv_batch_ragged_512_request_mix(gpu, ora, torch):
         keep += [din, dh]
         outs.append(dout)
         full.append((N, m, xp, hp))
-    batch = gpu.gb_create_conv_batch(creq, len(reqs), 0)
+    batch = gpu.gb_create_conv_batch(creq, len(reqs), 0, None)
     assert batch, gpu.gb_last_error_string()
     try:
         assert gpu.gb_execute_conv_batch(batch, torch.cuda.current_stream().cuda_stream) == 0

@@ -102,18 +102,15 @@ def test_large_batches_of_tiny_transforms(gpu, torch, N, B):
 def test_2d_column_schedules(gpu, mode, Nx, Ny):
     """2D columns as one pass of whole-column tiles (1) or as the two-pass
     four-step along the columns (2): c2c both directions, r2c and c2r."""
-    try:
-        assert gpu.gb_set_2d_columns(mode) == 0
-        x = signals.complex_uniform(75000 + Nx + Ny, Nx * Ny).reshape(Ny, Nx)
-        ref = np.fft.fft2(x.astype(np.complex128))
-        got = gpu.fft2_c2c(x, K.FORWARD)
-        assert rel_l2(got, ref) < 2e-6
-        inv = gpu.fft2_c2c(got, K.INVERSE)
-        assert rel_l2(inv / (Nx * Ny), x) < 4e-6
-        xr = signals.uniform(75100 + Nx + Ny, Nx * Ny).reshape(Ny, Nx)
-        X = gpu.fft2_r2c(xr)
-        assert rel_l2(X[:, : Nx // 2 + 1], np.fft.rfft2(xr.astype(np.float64))) < 2e-6
-        back = gpu.fft2_c2r(X)
-        assert rel_l2(back / (Nx * Ny), xr) < 4e-6
-    finally:
-        gpu.gb_set_2d_columns(0)
+    opts = gpu.options(columns_2d=mode)
+    x = signals.complex_uniform(75000 + Nx + Ny, Nx * Ny).reshape(Ny, Nx)
+    ref = np.fft.fft2(x.astype(np.complex128))
+    got = gpu.fft2_c2c(x, K.FORWARD, opts=opts)
+    assert rel_l2(got, ref) < 2e-6
+    inv = gpu.fft2_c2c(got, K.INVERSE, opts=opts)
+    assert rel_l2(inv / (Nx * Ny), x) < 4e-6
+    xr = signals.uniform(75100 + Nx + Ny, Nx * Ny).reshape(Ny, Nx)
+    X = gpu.fft2_r2c(xr, opts=opts)
+    assert rel_l2(X[:, : Nx // 2 + 1], np.fft.rfft2(xr.astype(np.float64))) < 2e-6
+    back = gpu.fft2_c2r(X, opts=opts)
+    assert rel_l2(back / (Nx * Ny), xr) < 4e-6

@@ -4,6 +4,8 @@ oracle is the FP64 DFT (numpy), and the plain FP32 path measured on the same
 input sets the error the three-limb form has to match."""
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -22,9 +24,8 @@ def gpu():
 
 @pytest.fixture(params=[0, 1], ids=["tcgen05", "mma.sync"])
 def engine(request, gpu):
-    assert gpu.gb_set_split_engine(request.param) == 0
-    yield request.param
-    gpu.gb_set_split_engine(0)
+    """Plan options selecting the split-precision engine."""
+    return gpu.options(split_engine=request.param)
 
 
 @pytest.fixture(scope="module")
@@ -34,11 +35,11 @@ def torch():
     return t
 
 
-def run(gpu, torch, x, direction, flags):
+def run(gpu, torch, x, direction, flags, opts=None):
     B, N = x.shape
     dx = torch.from_numpy(np.ascontiguousarray(x)).cuda()
     dy = torch.full_like(dx, complex(float("nan"), 0))
-    plan = gpu.gb_create_plan_1d_c2c_batched(N, direction, flags, B, 0, 0)
+    plan = gpu.gb_create_plan_1d(0, N, direction, flags, B, 0, 0, C.byref(opts) if opts else None)
     assert plan, gpu.gb_last_error_string()
     try:
         rc = gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), torch.cuda.current_stream().cuda_stream)
@@ -66,7 +67,7 @@ def inputs(kind, seed, B, N):
 def test_split_bf16x3_matches_fp32_error(gpu, torch, engine, N, B, direction, kind):
     x = inputs(kind, 40000 + N + B, B, N)
     ref = ref_f64(x, direction)
-    split = run(gpu, torch, x, direction, K.FLAG_SPLIT_BF16X3)
+    split = run(gpu, torch, x, direction, K.FLAG_SPLIT_BF16X3, engine)
     plain = run(gpu, torch, x, direction, 0)
     e_split, e_plain = rel_l2(split, ref), rel_l2(plain, ref)
     assert np.all(np.isfinite(split))
@@ -80,7 +81,7 @@ def test_split_bf16x3_matches_fp32_error(gpu, torch, engine, N, B, direction, ki
 def test_split_bf16x2_error(gpu, torch, engine, N, B, kind):
     x = inputs(kind, 41000 + N + B, B, N)
     for direction in (K.FORWARD, K.INVERSE):
-        got = run(gpu, torch, x, direction, K.FLAG_SPLIT_BF16X2)
+        got = run(gpu, torch, x, direction, K.FLAG_SPLIT_BF16X2, engine)
         e = rel_l2(got, ref_f64(x, direction))
         assert 1e-7 < e < 5e-5, e  # two limbs: ~16 significant bits
 
@@ -94,7 +95,7 @@ def test_split_strided_batch(gpu, torch, engine, N, dist):
     x[:, :N] = signals.complex_uniform(42000, B * N).reshape(B, N)
     dx = torch.from_numpy(x).cuda()
     dy = torch.zeros_like(dx)
-    plan = gpu.gb_create_plan_1d_c2c_batched(N, K.FORWARD, K.FLAG_SPLIT_BF16X3, B, dist, dist)
+    plan = gpu.gb_create_plan_1d(0, N, K.FORWARD, K.FLAG_SPLIT_BF16X3, B, dist, dist, C.byref(engine))
     assert plan
     assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(),
                                         torch.cuda.current_stream().cuda_stream) == 0

@@ -31,13 +31,8 @@ def linear_conv_f64(x, h):
 
 def stream(gpu, block, method, h, x, restart_at=None, fused=1, ranges=0):
     stereo = method & 1
-    assert gpu.gb_set_stream_conv_fused(fused) == 0
-    assert gpu.gb_set_stream_conv_ranges(ranges) == 0
-    try:
-        conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, len(h), 0)
-    finally:
-        gpu.gb_set_stream_conv_fused(1)
-        gpu.gb_set_stream_conv_ranges(0)
+    opts = gpu.options(stream_conv_fused=fused, stream_conv_ranges=ranges)
+    conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, len(h), 0, C.byref(opts))
     assert conv, gpu.gb_last_error_string()
     # one fused launch per block exactly when a 256-thread row tile holds the window
     M = 2 * block if stereo else block
@@ -121,7 +116,7 @@ def test_stream_conv_reset_restarts_history(gpu):
 def test_stream_conv_rejects_bad_arguments(gpu):
     h = np.ones(10, np.float32)
     for block, taps in ((1000, 10), (1, 10), (256, 0)):
-        assert not gpu.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0)
+        assert not gpu.gb_create_stream_conv(block, 0, h.ctypes.data, taps, 0, None)
         assert gpu.gb_last_error() == -1
         gpu.gb_clear_error()
 
@@ -137,7 +132,7 @@ def test_stream_conv_timeout_then_reset(gpu, method):
     sample = 8 if stereo else 4
     h = (signals.normal(65000, taps) * np.exp(-np.arange(taps) / (taps / 4))).astype(np.float32)
     x = signals.complex_uniform(65001, 14 * block) if stereo else signals.uniform(65001, 14 * block)
-    conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, taps, 0)
+    conv = gpu.gb_create_stream_conv(block, method, h.ctypes.data, taps, 0, None)
     assert conv, gpu.gb_last_error_string()
     try:
         assert gpu.gb_stream_conv_fused(conv) == 1
