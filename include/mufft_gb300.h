@@ -115,6 +115,10 @@ typedef struct mufft_gb_options {
      * sized to the GPU) and one launch per block (1) or a graph (0) */
     unsigned stream_conv_ranges;
     int stream_conv_fused;
+    /* ragged transform batches: requests of at least fft_split complex points
+     * (a power of two in 8192..65536; 0: none) run as four-step phase tasks
+     * over many CTAs, shorter ones above 4096 points whole in one CTA */
+    unsigned fft_split;
     /* preferred tile kernels (mufft_gb_list_tiles), first ntiles entries */
     unsigned ntiles;
     mufft_gb_tile_choice tiles[MUFFT_GB_MAX_TILE_CHOICES];
@@ -122,7 +126,7 @@ typedef struct mufft_gb_options {
 
 /* The defaults: levels 0, twiddles -1, fused 0, tma 0, occupancy 0, stream
  * tiles 0, split engine 0, 2D columns 0, conv_split 65536, conv_classes
- * 16384, stream ranges 0, stream fused 1, no tile choices. */
+ * 16384, stream ranges 0, stream fused 1, fft_split 8192, no tile choices. */
 void mufft_gb_options_init(mufft_gb_options *opts);
 
 /* 1D plans of every kind with options: kind 0 c2c, 1 r2c, 2 c2r (direction
@@ -258,6 +262,49 @@ int mufft_gb_conv_batch_status(mufft_gb_conv_batch *batch);
  * batch must not overlap on the GPU (they share its scratch). */
 int mufft_gb_execute_conv_batch(mufft_gb_conv_batch *batch, void *stream);
 void mufft_gb_free_conv_batch(mufft_gb_conv_batch *batch);
+
+/* ---------------------------------------------- ragged batched transforms */
+
+/* No counterpart in the reference, which runs one transform per plan execute
+ * (fft.c:811-850).  One request is what a plan of its kind, N and flags does
+ * in one mufft_execute_plan_1d: kind 0 c2c (direction MUFFT_FORWARD or
+ * MUFFT_INVERSE), 1 r2c, 2 c2r; flags MUFFT_FLAG_ZERO_PAD_UPPER_HALF and (r2c)
+ * MUFFT_FLAG_FULL_R2C, the CPU flags accepted and ignored; unnormalised.
+ *   N: power of two; c2c 2..65536, r2c and c2r 4..131072.
+ *   input / output: device memory, 8-byte aligned, sized as for a plan (c2c
+ *     N complex in, N/2 with zero padding, N out; r2c N (N/2) reals in, N/2+1
+ *     (N with FULL_R2C) complex out; c2r N/2+1 complex in, N reals out);
+ *     the addresses are fixed when the batch is created. */
+typedef struct mufft_gb_fft_request {
+    unsigned N;
+    int kind;
+    int direction;
+    unsigned flags;
+    const void *input;
+    void *output;
+} mufft_gb_fft_request;
+
+typedef struct mufft_gb_fft_batch mufft_gb_fft_batch;
+
+/* Prepares `count` requests of mixed kinds and sizes for one persistent
+ * launch captured in a CUDA graph.  Requests of up to 4096 complex points run
+ * in groups of one class as the transforms of one tile; longer ones as
+ * four-step phase tasks that any CTA may take.  flags: 0, or
+ * MUFFT_GB_FLAG_AUTOTUNE to time the batch with every split size and grid
+ * (running it, so writing the outputs, a few times) and keep the fastest.
+ * opts: NULL for the defaults. */
+mufft_gb_fft_batch *mufft_gb_create_fft_batch(const mufft_gb_fft_request *requests, unsigned count, unsigned flags,
+                                              const mufft_gb_options *opts);
+/* Replays the batch on `stream` (enqueued, not synchronised).  Executes of one
+ * batch must not overlap on the GPU (they share its scratch and counters). */
+int mufft_gb_execute_fft_batch(mufft_gb_fft_batch *batch, void *stream);
+/* Synchronises the device and reports whether a bounded wait of the batch's
+ * task dependencies timed out in an earlier execute (MUFFT_GB_ERR_UNSUPPORTED),
+ * clearing the flag. */
+int mufft_gb_fft_batch_status(mufft_gb_fft_batch *batch);
+/* "requests=.. tasks=.. split=.. grid=.. resident=.. algorithmic_bytes=.." */
+int mufft_gb_fft_batch_describe(const mufft_gb_fft_batch *batch, char *buf, size_t size);
+void mufft_gb_free_fft_batch(mufft_gb_fft_batch *batch);
 
 /* ---------------------------------------------- streaming convolution */
 

@@ -113,6 +113,11 @@ GB_H = [
     ("conv_batch_class_size", _u, [_vp]),
     ("conv_batch_status", _i, [_vp]),
     ("free_conv_batch", None, [_vp]),
+    ("create_fft_batch", _vp, [_vp, _u, _u, _vp]),
+    ("execute_fft_batch", _i, [_vp, _vp]),
+    ("fft_batch_status", _i, [_vp]),
+    ("fft_batch_describe", _i, [_vp, C.c_char_p, _sz]),
+    ("free_fft_batch", None, [_vp]),
     ("device_alloc", _vp, [_sz]),
     ("device_free", None, [_vp]),
     ("memcpy", _i, [_vp, _vp, _sz]),
@@ -126,6 +131,12 @@ class ConvRequest(C.Structure):
     """mufft_gb_conv_request (include/mufft_gb300.h)."""
     _fields_ = [("N", C.c_uint), ("method", C.c_uint), ("input", C.c_void_p), ("filter", C.c_void_p),
                 ("output", C.c_void_p)]
+
+
+class FftRequest(C.Structure):
+    """mufft_gb_fft_request (include/mufft_gb300.h)."""
+    _fields_ = [("N", C.c_uint), ("kind", C.c_int), ("direction", C.c_int), ("flags", C.c_uint),
+                ("input", C.c_void_p), ("output", C.c_void_p)]
 
 
 class TileChoice(C.Structure):
@@ -143,7 +154,7 @@ class Options(C.Structure):
                 ("fused_passes", C.c_int), ("tma", C.c_int), ("tile_occupancy", C.c_int), ("stream_tiles", C.c_int),
                 ("split_engine", C.c_int), ("columns_2d", C.c_int), ("conv_split", C.c_uint),
                 ("conv_classes", C.c_uint), ("stream_conv_ranges", C.c_uint), ("stream_conv_fused", C.c_int),
-                ("ntiles", C.c_uint), ("tiles", TileChoice * MAX_TILE_CHOICES)]
+                ("fft_split", C.c_uint), ("ntiles", C.c_uint), ("tiles", TileChoice * MAX_TILE_CHOICES)]
 
 
 class MuFFTError(RuntimeError):

@@ -182,6 +182,8 @@ bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
         bad = "at most 2^20 partition ranges";
     else if (o->stream_conv_fused < 0 || o->stream_conv_fused > 1)
         bad = "stream_conv_fused must be 0 or 1";
+    else if (o->fft_split != 0 && (!is_pow2(o->fft_split) || o->fft_split < 8192 || o->fft_split > 65536))
+        bad = "fft_split must be 0 or a power of two in 8192..65536";
     else if (o->ntiles > MUFFT_GB_MAX_TILE_CHOICES)
         bad = "at most MUFFT_GB_MAX_TILE_CHOICES tile choices";
     if (bad) {
@@ -343,6 +345,7 @@ void mufft_gb_options_init(mufft_gb_options *o)
     o->conv_classes = 16384;
     o->stream_conv_ranges = 0;
     o->stream_conv_fused = 1;
+    o->fft_split = 8192;
 }
 
 // ================================================================ memory

@@ -69,3 +69,38 @@ def ragged_conv_requests(seed: int = 4, count: int = 512):
         x = complex_uniform(20000 + i, N // 2) if stereo[i] else uniform(20000 + i, N // 2)
         reqs.append((N, bool(stereo[i]), x, h))
     return reqs
+
+
+def ragged_fft_requests(seed: int = 6, count: int = 512, lo: int = 4, hi: int = 16):
+    """The ragged transform mix: `count` requests with N = 2^e, e uniform on
+    lo..hi (numpy Generator `seed`); the kind is c2c forward, c2c inverse, r2c
+    or c2r with equal odds; a quarter of the c2c and r2c requests zero-pad the
+    upper half of their input, half of the r2c requests write all N bins
+    (FULL_R2C).  Request i's input (SplitMix64 seed 30000 + i) is uniform on
+    [-1, 1): N complex (N/2 with zero padding) for c2c, N reals (N/2) for
+    r2c, N/2 + 1 complex for c2r.  Returns (N, kind, direction, flags, input)
+    tuples with the fft.h flag values."""
+    rng = np.random.default_rng(seed)
+    e = rng.integers(lo, hi + 1, count)
+    choice = rng.integers(0, 4, count)
+    zp = rng.random(count) < 0.25
+    full = rng.random(count) < 0.5
+    reqs = []
+    for i in range(count):
+        N = 1 << int(e[i])
+        kind = 0 if choice[i] < 2 else int(choice[i]) - 1
+        direction = 1 if choice[i] == 1 else -1
+        flags = 0
+        if kind != 2 and zp[i]:
+            flags |= 1 << 17       # MUFFT_FLAG_ZERO_PAD_UPPER_HALF
+        if kind == 1 and full[i]:
+            flags |= 1 << 16       # MUFFT_FLAG_FULL_R2C
+        n_in = N // 2 if flags & (1 << 17) else N
+        if kind == 0:
+            x = complex_uniform(30000 + i, n_in)
+        elif kind == 1:
+            x = uniform(30000 + i, n_in)
+        else:
+            x = complex_uniform(30000 + i, N // 2 + 1)
+        reqs.append((N, kind, direction, flags, x))
+    return reqs

@@ -268,3 +268,34 @@ def test_batched_convolution_entry_points_validate_on_host(lib):
     assert lib.gb_stream_conv_ranges(None) == 0 and lib.gb_stream_conv_fused(None) == 0
     assert lib.gb_stream_conv_status(None) == -1
     lib.gb_clear_error()
+
+
+def test_fft_batch_validates_requests_on_host(lib):
+    """Request checks run before any device work (no GPU needed)."""
+    fake = 0x10000
+    cases = [(1000, 0, -1, 0, fake, fake, -1),          # not a power of two
+             (2, 1, -1, 0, fake, fake, -1),             # real kinds need N >= 4
+             (1024, 3, -1, 0, fake, fake, -1),          # no such kind
+             (1024, 0, 0, 0, fake, fake, -1),           # c2c direction
+             (1024, 0, -1, 1 << 24, fake, fake, -1),    # flag the batch does not take
+             (1024, 0, -1, 0, fake + 4, fake, -1),      # misaligned input
+             (1024, 0, -1, 0, None, fake, -1),
+             (1 << 17, 0, -1, 0, fake, fake, -2),       # c2c longer than 65536
+             (1 << 18, 1, -1, 0, fake, fake, -2)]       # r2c longer than 131072
+    for N, kind, direction, flags, pin, pout, code in cases:
+        reqs = (K.FftRequest * 1)(K.FftRequest(N, kind, direction, flags, pin, pout))
+        assert not lib.gb_create_fft_batch(reqs, 1, 0, None)
+        assert lib.gb_last_error() == code, (N, kind, direction, flags)
+        lib.gb_clear_error()
+    assert not lib.gb_create_fft_batch(None, 0, 0, None)
+    assert lib.gb_last_error() == -1
+    lib.gb_clear_error()
+    bad = lib.options(fft_split=4096)
+    reqs = (K.FftRequest * 1)(K.FftRequest(1024, 0, -1, 0, fake, fake))
+    assert not lib.gb_create_fft_batch(reqs, 1, 0, C.byref(bad))
+    assert lib.gb_last_error() == -1
+    lib.gb_clear_error()
+    assert lib.gb_execute_fft_batch(None, None) == -1
+    assert lib.gb_fft_batch_status(None) == -1
+    lib.gb_clear_error()
+    lib.gb_free_fft_batch(None)
