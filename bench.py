@@ -274,11 +274,13 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
             torch.cuda.synchronize()
         barrier(pg)
         torch.cuda.synchronize()
+        torch.cuda.profiler.start()  # the capture range of `ncu --profile-from-start off`
         ev0.record(st)
         for i in range(args.steps):
             step(args.warmup + i)
         ev1.record(st)
         torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
         barrier(pg)
     ms = ev0.elapsed_time(ev1)
     ms_max = max_over_ranks(pg, ms)
@@ -843,6 +845,113 @@ COMPANIONS = {
 }
 
 
+# ------------------------------------------------------------ profiling cases
+#
+# `python bench.py --profile-case NAME`: one small workload, warmed up, then
+# one iteration inside cudaProfilerStart/Stop, for `ncu --profile-from-start
+# off` captures of the kernels that the headline line does not run.
+
+def profile_case(name: str) -> None:
+    import torch
+
+    import mufft_gb300
+    from mufft_gb300 import capi as K
+    from mufft_gb300 import signals
+    lib = mufft_gb300.load()
+    sp = torch.cuda.current_stream().cuda_stream
+    PADS = K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_FIRST | K.CONV_METHOD_FLAG_ZERO_PAD_UPPER_HALF_SECOND
+    keep = []
+
+    def region(fn, warm=2):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        fn()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+
+    if name == "c2c_1024x4096":  # batch 4096 x c2c N=1024 (32 MiB per buffer), the tuned schedule
+        N, B = 1024, 4096
+        lib.gb_autotune_1d(0, N, -1, 0, B, None, 0)
+        p = lib.gb_create_plan_1d_c2c_batched(N, -1, 0, B, 0, 0)
+        x = torch.from_numpy(signals.complex_uniform(1, N * B)).cuda()
+        y = torch.empty_like(x)
+        region(lambda: lib.gb_execute_plan_1d_async(p, y.data_ptr(), x.data_ptr(), sp))
+    elif name == "fft2d_4096":  # 4096 x 4096 r2c then c2r
+        Nx = Ny = 4096
+        x = torch.randn(Nx * Ny, device="cuda")
+        X = torch.empty(Nx * Ny, dtype=torch.complex64, device="cuda")
+        y = torch.empty(2 * Nx * Ny, device="cuda")
+        pf, pb = lib.create_plan_2d_r2c(Nx, Ny, 0), lib.create_plan_2d_c2r(Nx, Ny, 0)
+
+        def f():
+            lib.gb_execute_plan_2d_async(pf, X.data_ptr(), x.data_ptr(), sp)
+            lib.gb_execute_plan_2d_async(pb, y.data_ptr(), X.data_ptr(), sp)
+        region(f)
+    elif name in ("conv_2e21", "adjoint_2e21x8"):
+        N = 1 << 21
+        p = lib.create_plan_conv(N, 0, K.CONV_METHOD_FLAG_STEREO_MONO | PADS)
+        nb = lib.conv_get_transformed_block_size(p) // 8
+        if name == "conv_2e21":  # one stereo convolution: input FIRST, SECOND, output
+            x = torch.zeros(N, dtype=torch.complex64, device="cuda")
+            x[: N // 2] = torch.from_numpy(signals.complex_uniform(3, N // 2)).cuda()
+            h = torch.zeros(N, device="cuda")
+            h[:65536] = torch.randn(65536, device="cuda")
+            A, H = torch.empty(nb, dtype=torch.complex64, device="cuda"), torch.empty(nb, dtype=torch.complex64,
+                                                                                     device="cuda")
+            out = torch.empty(N, dtype=torch.complex64, device="cuda")
+
+            def f():
+                lib.gb_execute_conv_input_async(p, K.CONV_BLOCK_FIRST, A.data_ptr(), x.data_ptr(), sp)
+                lib.gb_execute_conv_input_async(p, K.CONV_BLOCK_SECOND, H.data_ptr(), h.data_ptr(), sp)
+                lib.gb_execute_conv_output_async(p, out.data_ptr(), A.data_ptr(), H.data_ptr(), sp)
+        else:  # one gradient step's kernels for 8 stereo signals: batched outputs + both adjoints
+            B = 8
+            A = torch.randn((B, nb), dtype=torch.complex64, device="cuda")
+            H = torch.randn(nb, dtype=torch.complex64, device="cuda")
+            r = torch.randn((B, N), dtype=torch.complex64, device="cuda")
+            y, gx, gh = torch.empty_like(r), torch.empty_like(r), torch.empty(N, device="cuda")
+
+            def f():
+                lib.gb_execute_conv_output_batched(p, y.data_ptr(), N, A.data_ptr(), nb, H.data_ptr(), B, sp)
+                lib.gb_conv_adjoint(p, gh.data_ptr(), gx.data_ptr(), N, r.data_ptr(), N, A.data_ptr(), nb,
+                                    H.data_ptr(), B, sp)
+        region(f)
+    elif name == "ragged_fft_512":  # the 512-request transform batch
+        reqs = signals.ragged_fft_requests(6, 512)
+        creq = (K.FftRequest * len(reqs))()
+        for i, (N, kind, d, fl, x) in enumerate(reqs):
+            din = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+            nout = N if kind == 0 or (kind == 1 and fl & K.FLAG_FULL_R2C) else (N // 2 + 1 if kind == 1 else N)
+            dout = torch.empty(nout, dtype=torch.float32 if kind == 2 else torch.complex64, device="cuda")
+            keep.extend([din, dout])
+            creq[i] = K.FftRequest(N, kind, d, fl, din.data_ptr(), dout.data_ptr())
+        b = lib.gb_create_fft_batch(creq, len(reqs), 0, None)
+        region(lambda: lib.gb_execute_fft_batch(b, sp))
+        assert lib.gb_fft_batch_status(b) == 0
+    elif name == "ragged_conv_512":  # the 512-request convolution batch
+        reqs = signals.ragged_conv_requests(4, 512)
+        creq = (K.ConvRequest * len(reqs))()
+        for i, (N, stereo, x, h) in enumerate(reqs):
+            m = PADS | (1 if stereo else 0)
+            nblk = N if stereo else N // 2 + 4
+            din = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+            dH = torch.randn(nblk, dtype=torch.complex64, device="cuda")
+            dout = torch.empty(N, dtype=torch.complex64 if stereo else torch.float32, device="cuda")
+            keep.extend([din, dH, dout])
+            creq[i] = K.ConvRequest(N, m, din.data_ptr(), dH.data_ptr(), dout.data_ptr())
+        b = lib.gb_create_conv_batch(creq, len(reqs), 0, None)
+        region(lambda: lib.gb_execute_conv_batch(b, sp))
+        assert lib.gb_conv_batch_status(b) == 0
+    else:
+        raise SystemExit(f"unknown profile case {name}")
+    print(json.dumps({"profile_case": name, "ok": True}))
+
+
+PROFILE_CASES = ("c2c_1024x4096", "fft2d_4096", "conv_2e21", "adjoint_2e21x8", "ragged_fft_512", "ragged_conv_512")
+
+
 def run_reference(args, world, rank, pg) -> dict | None:
     if rank != 0:
         return None
@@ -881,7 +990,12 @@ def main():
                     help="skip the split-precision, ragged-convolution and adjoint measurements")
     ap.add_argument("--companions", default="all",
                     help="comma-separated companion measurements to run (default all: " + ",".join(COMPANIONS) + ")")
+    ap.add_argument("--profile-case", choices=PROFILE_CASES,
+                    help="run one small workload inside a profiler range (for ncu) and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     args.warmup = max(3, args.warmup)
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
