@@ -107,9 +107,9 @@ typedef struct mufft_gb_options {
      * of short, wide column tiles), 1 one pass, 2 two passes where possible */
     int columns_2d;
     /* ragged convolution batches: requests of at least conv_split complex
-     * points (a power of two in 8192..65536; 0: none) run as phase tasks over
-     * many CTAs, of at least conv_classes points (16384..65536; 0: none) as
-     * class pipelines */
+     * points run as phase tasks over many CTAs (0: none), of at least
+     * conv_classes points as class pipelines (0: none); powers of two in
+     * 16384..65536 */
     unsigned conv_split, conv_classes;
     /* streaming convolution: partition ranges of the multiply-accumulate (0
      * sized to the GPU) and one launch per block (1) or a graph (0) */

@@ -157,18 +157,15 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
     std::map<std::tuple<unsigned, unsigned, unsigned>, std::vector<unsigned>> classes;
     unsigned nsplit = 0;
     for (unsigned i = 0; i < reqs.size(); i++) {
-        if (reqs[i].lg >= class_lg && reqs[i].lg >= kRaggedMinClassLg) {
+        if (reqs[i].lg >= class_lg && reqs[i].lg >= kRaggedMinSplitLg) {
             classes[std::make_tuple(reqs[i].lg, reqs[i].stereo, reqs[i].zero_pad)].push_back(i);
             continue;
         }
-        // four-step requests: one task per tile / chunk of each phase from the
-        // split size on, one task per phase below it; all wait on a counter
-        if (reqs[i].lg >= kRaggedMinSplitLg) {
-            reqs[i].split = reqs[i].lg >= split_lg ? 1 : 0;
+        reqs[i].split = reqs[i].lg >= split_lg && reqs[i].lg >= kRaggedMinSplitLg ? 1 : 0;
+        if (reqs[i].split) {
             reqs[i].counter = 1 + nsplit++;
             split_ids.push_back(i);
         } else {
-            reqs[i].split = 0;
             whole_ids.push_back(i);
         }
     }
@@ -194,6 +191,10 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
         };
         for (unsigned r : whole_ids) {
             const unsigned gs = ragged_group_size(reqs[r].lg);
+            if (gs <= 1) {
+                whole.push_back(RaggedTask{r, 0, 0, 0, 0});
+                continue;
+            }
             std::vector<unsigned> &g = open[std::make_tuple(reqs[r].lg, reqs[r].stereo, reqs[r].zero_pad)];
             g.push_back(r);
             if (g.size() == gs)
@@ -207,22 +208,16 @@ bool conv_batch_build(mufft_gb_conv_batch *b, unsigned split_lg, unsigned class_
             return reqs[x.req].lg > reqs[y.req].lg;
         });
     }
-    // phase-major over four-step requests, with group tasks (longest first) in between
+    // phase-major over split requests, with whole requests (longest first) in between
     std::vector<RaggedTask> tasks;
     size_t w = 0;
-    auto phase_tasks = [&](unsigned r, unsigned p) {
-        const unsigned n = ragged_phase_tasks(reqs[r].lg, p, reqs[r].stereo);
-        return reqs[r].split ? n : (n ? 1u : 0u);
-    };
     for (unsigned phase = 0; phase < 5; phase++) {
         for (unsigned r : split_ids) {
             unsigned before = 0;
             for (unsigned p = 0; p < phase; p++)
-                before += phase_tasks(r, p);
-            const unsigned n = phase_tasks(r, phase);
-            for (unsigned t = 0; t < n; t++)
-                tasks.push_back(RaggedTask{r, (unsigned short)phase,
-                                           reqs[r].split ? (unsigned short)t : kRaggedWholePhase, before, 0});
+                before += ragged_phase_tasks(reqs[r].lg, p);
+            for (unsigned t = 0; t < ragged_phase_tasks(reqs[r].lg, phase); t++)
+                tasks.push_back(RaggedTask{r, (unsigned short)phase, (unsigned short)t, before, 0});
         }
         const size_t take = phase == 4 ? whole.size() - w : (whole.size() - w) / (5 - phase);
         for (size_t k = 0; k < take; k++, w++)
@@ -422,7 +417,7 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
         std::vector<Cand> cands;
         for (unsigned lg = kRaggedMinSplitLg; lg <= 17; lg++)
             cands.push_back(Cand{lg, 17, 0});
-        for (unsigned cl = kRaggedMinClassLg; cl <= 16; cl++)
+        for (unsigned cl = kRaggedMinSplitLg; cl <= 16; cl++)
             for (unsigned div : {1u, 2u, 4u})
                 cands.push_back(Cand{17, cl, (unsigned)b->sms / div});
         Cand best_c{best_lg, best_class, 0};

@@ -8,28 +8,26 @@
 // goes through an N/2-point complex FFT with the r2c/c2r fix-ups,
 // STEREO_MONO through an N-point complex FFT (fft.c:585-599).
 //
-// Every CTA (256 threads, several per SM) takes the next work item from a
-// global counter; the host orders the items longest first.
-//   Complex length L <= 4096: requests of one (size, method, zero-pad) class
-//     run in groups, the C transforms of one tile pair (C = 4096 / L) each
-//     taking its request's buffers from tables: a forward tile (r2c fix-up
-//     fused into its store for mono) writes the spectra to the requests'
-//     scratch, which stays in L2; an inverse tile reads them back with the
-//     multiply and the c2r pre-pass fused into its loads.
-//   L = 8192 .. 65536: a four-step L = L1 x L2 over the request's scratch.
-//     The forward half stops at the transposed spectrum
+// Every CTA (512 threads) takes the next work item from a global counter.
+// The host orders the items (longest requests first) and decides which
+// requests are split: a split request of L = L1 x L2 >= 16384 points runs as
+// five phases of tasks (F1 column tiles, F2 row tiles, multiply chunks, I1 row
+// tiles, I2 column tiles) that any CTA may take, each task waiting (bounded)
+// on a per-request counter until the previous phase is complete; phases are
+// queued phase-major across requests, so the waits are rarely long, and every
+// awaited task was dequeued earlier by a running CTA (no deadlock).  A request
+// that is not split runs whole in one CTA:
+//   L <= 8192 complex points: one forward tile (r2c fix-up fused into its
+//     store for mono) writes the spectrum to the request's scratch, which
+//     stays in L2; one inverse tile reads it back with the multiply and the
+//     c2r pre-pass fused into its loads.
+//   L = 16384 .. 65536: an in-CTA four-step over the request's scratch,
+//     L = L1 x L2.  The forward half stops at the transposed spectrum
 //     X^T[k1][k2] = X[k1 + L1*k2] (no transpose), the multiply (and for mono
 //     the r2c fix-up, product and c2r pre-pass of each bin pair k, L-k) runs
 //     on that layout, and the inverse four-step consumes it directly:
-//       F1 columns of L1 with W_L^(n2*k1) -> F2 rows of L2 (stereo: times
-//       H / N in their store) -> multiply (mono) -> I1 rows of L2 (inverse)
-//       with W_L^(-n2*k1) -> I2 columns of L1 -> output.
-//     Each phase is a set of tasks that any CTA may take (from the split size
-//     on, one per tile or chunk; below it, one task per phase), each waiting
-//     (bounded) on a per-request counter until the previous phase is
-//     complete; phases are queued phase-major across requests, group tasks in
-//     between, and every awaited task was dequeued earlier by a running CTA
-//     (no deadlock).
+//       F1 columns of L1 with W_L^(n2*k1) -> F2 rows of L2 -> multiply ->
+//       I1 rows of L2 (inverse) with W_L^(-n2*k1) -> I2 columns of L1 -> output.
 #include "../../include/fft.h"
 #include "conv_ragged.h"
 #include "fft_device.cuh"
@@ -38,50 +36,82 @@ namespace mgb {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 
-template <int L> __host__ __device__ constexpr int grp_c() { return kThreads * 16 / L; }
+template <int L> __host__ __device__ constexpr int single_r() { return L > 8192 ? 32 : 16; }
+template <int L> __host__ __device__ constexpr int single_c() { return kThreads * single_r<L>() / L; }
 
-// Four-step split of 2^lg points: L1 (columns) x L2 (rows).
-__host__ __device__ constexpr unsigned cr_l1(unsigned lg) { return lg == 13 ? 64 : (lg == 16 ? 256 : 128); }
-__host__ __device__ constexpr unsigned cr_l2(unsigned lg) { return lg >= 15 ? 256 : 128; }
-
-// A group of n whole requests of one class: the n transforms of one tile pair
-// (the tile's C transforms each take one request's buffers from the tables).
-// The two halves are separate calls so that nothing stays live across them.
+// Forward tile into the spectrum scratch, then the fused multiply + inverse
+// tile into the output.
 template <int L>
-__device__ __noinline__ void conv_group_fwd(const RaggedReq &q, const float2 *const *tab, unsigned n, float2 *smem,
-                                            const float2 *tw, const float2 *rtw_fwd)
+__device__ void conv_single(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
+                            const float2 *rtw_inv)
 {
-    constexpr int C = grp_c<L>();
+    constexpr int C = single_c<L>(), R = single_r<L>();
+    const bool mono = q.stereo == 0;
     TileArgs f{};
     f.in = q.in;
     f.out = q.spec;
-    f.in_tab = tab;
-    f.out_tab = (float2 *const *)(tab + 3 * n);
     f.in_stride = f.out_stride = 1;
-    f.ntrans = n;
+    f.in_dist = f.out_dist = L + 1;
+    f.ntrans = 1;
     f.half = q.zero_pad;
-    f.epilogue = q.stereo ? EPI_PLAIN : EPI_R2C;
+    f.epilogue = mono ? EPI_R2C : EPI_PLAIN;
     f.tw = tw;
     f.rtw = rtw_fwd;
     f.scale = 1.0f;
-    tile_body<L, 16, C, 1, ALONG, ALONG, false, false, false, false, false, true>(f, 0, 0, 0, 0, smem);
-}
+    tile_body<L, R, C, 1, ALONG, ALONG, false>(f, 0, 0, 0, 0, smem);
+    __syncthreads();  // spectrum complete and visible to the whole CTA
 
-template <int L>
-__device__ __noinline__ void conv_group_inv(const RaggedReq &q, const float2 *const *tab, unsigned n, float2 *smem,
-                                            const float2 *tw, const float2 *rtw_inv)
-{
-    constexpr int C = grp_c<L>();
-    const bool mono = q.stereo == 0;
     TileArgs b{};
     b.in = q.spec;
     b.in2 = q.h;
     b.out = q.out;
-    b.in_tab = tab + 3 * n;
-    b.in2_tab = tab + n;
-    b.out_tab = (float2 *const *)(tab + 2 * n);
+    b.in_stride = b.out_stride = 1;
+    b.in_dist = b.out_dist = L + 1;
+    b.ntrans = 1;
+    b.prologue = mono ? PRO_MUL_C2R : PRO_MUL;
+    b.mirror_len = L;
+    b.rtw = rtw_inv;
+    b.scale = q.scale;
+    b.conj = 3;
+    b.tw = tw;
+    tile_body<L, R, C, 1, ALONG, ALONG, true>(b, 0, 0, 0, 0, smem);
+    __syncthreads();
+}
+
+// A group of n whole requests of one class: the n transforms of one tile pair
+// (the tile's C transforms each take one request's buffers from the tables).
+template <int L>
+__device__ void conv_group(const RaggedReq &q, const float2 *const *tab, unsigned n, float2 *smem, const float2 *tw,
+                           const float2 *rtw_fwd, const float2 *rtw_inv)
+{
+    constexpr int C = single_c<L>(), R = single_r<L>();
+    const bool mono = q.stereo == 0;
+    const float2 *const *t_in = tab, *const *t_h = tab + n;
+    float2 *const *t_out = (float2 *const *)(tab + 2 * n), *const *t_spec = (float2 *const *)(tab + 3 * n);
+    TileArgs f{};
+    f.in = q.in;
+    f.out = q.spec;
+    f.in_tab = t_in;
+    f.out_tab = t_spec;
+    f.in_stride = f.out_stride = 1;
+    f.ntrans = n;
+    f.half = q.zero_pad;
+    f.epilogue = mono ? EPI_R2C : EPI_PLAIN;
+    f.tw = tw;
+    f.rtw = rtw_fwd;
+    f.scale = 1.0f;
+    tile_body<L, R, C, 1, ALONG, ALONG, false, false, false, false, false, true>(f, 0, 0, 0, 0, smem);
+    __syncthreads();  // spectra complete and visible to the whole CTA
+
+    TileArgs b{};
+    b.in = q.spec;
+    b.in2 = q.h;
+    b.out = q.out;
+    b.in_tab = (const float2 *const *)t_spec;
+    b.in2_tab = t_h;
+    b.out_tab = t_out;
     b.in_stride = b.out_stride = 1;
     b.ntrans = n;
     b.prologue = mono ? PRO_MUL_C2R : PRO_MUL;
@@ -90,40 +120,29 @@ __device__ __noinline__ void conv_group_inv(const RaggedReq &q, const float2 *co
     b.scale = q.scale;
     b.conj = 3;
     b.tw = tw;
-    if constexpr (Sched<L, 16>::NST > 1) {
-        // mono: the spectrum row is staged in shared memory once, so each bin is
-        // loaded once instead of twice (for its own output and its mirror's)
-        if (mono)
-            tile_body<L, 16, C, 1, ALONG, ALONG, true, false, false, true, false, true>(b, 0, 0, 0, 0, smem);
-        else
-            tile_body<L, 16, C, 1, ALONG, ALONG, true, false, false, false, false, true>(b, 0, 0, 0, 0, smem);
-    } else {
-        tile_body<L, 16, C, 1, ALONG, ALONG, true, false, false, false, false, true>(b, 0, 0, 0, 0, smem);
-    }
-}
-
-// Tables: n inputs, n filter spectra, n outputs, n spectrum scratch slots.
-template <int L>
-__device__ void conv_group(const RaggedReq &q, const float2 *const *tab, unsigned n, float2 *smem, const float2 *tw,
-                           const float2 *rtw_fwd, const float2 *rtw_inv)
-{
-    conv_group_fwd<L>(q, tab, n, smem, tw, rtw_fwd);
-    __syncthreads();  // spectra complete and visible to the whole CTA
-    conv_group_inv<L>(q, tab, n, smem, tw, rtw_inv);
+    tile_body<L, R, C, 1, ALONG, ALONG, true, false, false, false, false, true>(b, 0, 0, 0, 0, smem);
     __syncthreads();
 }
 
-// Multiply phase of a mono request on the transposed spectrum, chunk `chunk`
-// of `nchunks` of the bin pairs k, L-k (k = 0 .. L/2):
-// Z (forward complex FFT of the packed reals) -> r2c bins X -> Y = s*X*H ->
-// c2r pre-pass Zi, pair by pair (kernel.c:36-82).
+// Multiply phase of the four-step path on the transposed spectrum, for the
+// chunk `chunk` of `nchunks` (pairs k, L-k for mono; elements for stereo).
 template <int L1, int L2>
-__device__ void conv_multiply_mono(const RaggedReq &q, const float2 *rtw_fwd, const float2 *rtw_inv, unsigned chunk,
-                                   unsigned nchunks)
+__device__ void conv_multiply(const RaggedReq &q, const float2 *rtw_fwd, const float2 *rtw_inv, unsigned chunk,
+                              unsigned nchunks)
 {
     constexpr int L = L1 * L2;
     float2 *s = q.spec;
     auto at = [](int k) { return (k % L1) * L2 + k / L1; };  // X[k] lives at X^T[k % L1][k / L1]
+    if (q.stereo) {
+        const int i0 = (int)((long long)L * chunk / nchunks), i1 = (int)((long long)L * (chunk + 1) / nchunks);
+        for (int idx = i0 + threadIdx.x; idx < i1; idx += kThreads) {
+            const int k = (idx / L2) + L1 * (idx % L2);
+            s[idx] = cscale(cmul(__ldcg(&s[idx]), __ldcg(&q.h[k])), q.scale);
+        }
+        return;
+    }
+    // mono: Z (forward complex FFT of the packed reals) -> r2c bins X -> Y = s*X*H
+    // -> c2r pre-pass Zi, pair by pair (kernel.c:36-82).
     constexpr int NP = L / 2 + 1;
     const int k0 = (int)((long long)NP * chunk / nchunks), k1 = (int)((long long)NP * (chunk + 1) / nchunks);
     for (int k = k0 + threadIdx.x; k < k1; k += kThreads) {
@@ -149,6 +168,9 @@ __device__ void conv_multiply_mono(const RaggedReq &q, const float2 *rtw_fwd, co
     }
 }
 
+template <int L1, int L2> __host__ __device__ constexpr int c1_of() { return kThreads * 16 / L1; }
+template <int L1, int L2> __host__ __device__ constexpr int c2_of() { return kThreads * 16 / L2; }
+
 // Tile arguments of the four phases that transform (F1, F2, I1, I2).
 template <int L1, int L2>
 __device__ TileArgs multi_args(const RaggedReq &q, const float2 *tw, int phase)
@@ -168,11 +190,10 @@ __device__ TileArgs multi_args(const RaggedReq &q, const float2 *tw, int phase)
         a.ntrans = L2;
         a.half = phase == 0 ? q.zero_pad : 0;
         a.epilogue = phase == 0 ? EPI_TWIDDLE : EPI_PLAIN;
-        a.tw_colpow = phase == 0 ? 1 : 0;
         a.conj = phase == 0 ? 0 : 2;  // I2: inverse over k1 of conj(Z), conjugated out
     } else {
         // rows of length L2, in place; I1: inverse over k2 (conj in, forward FFT,
-        // W_L^(n2*k1)) -> conj(Z); F2 of a stereo request: times s * H[k1 + L1*k2]
+        // W_L^(n2*k1)) -> conj(Z)
         a.in = q.spec;
         a.out = q.spec;
         a.in_stride = a.out_stride = 1;
@@ -180,39 +201,51 @@ __device__ TileArgs multi_args(const RaggedReq &q, const float2 *tw, int phase)
         a.ntrans = L1;
         a.conj = phase == 3 ? 1 : 0;
         a.epilogue = phase == 3 ? EPI_TWIDDLE : EPI_PLAIN;
-        if (phase == 1 && q.stereo) {
-            a.in2 = q.h;
-            a.in2_dist = 1;
-            a.in2_stride = L1;
-            a.scale = q.scale;
-        }
     }
     return a;
 }
 
-// One tile (or multiply chunk) `index` of phase `phase` of a four-step request.
+// One phase task of a split request (or, with index < 0, the whole phase).
 template <int L1, int L2>
 __device__ void multi_phase(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
                             const float2 *rtw_inv, int phase, int index)
 {
-    constexpr int C1 = kThreads * 16 / L1, C2 = kThreads * 16 / L2;
+    constexpr int C1 = c1_of<L1, L2>(), C2 = c2_of<L1, L2>();
     if (phase == 2) {
-        if (!q.stereo)
-            conv_multiply_mono<L1, L2>(q, rtw_fwd, rtw_inv, (unsigned)index, kRaggedMulChunks);
-        __syncthreads();
+        if (index < 0)
+            conv_multiply<L1, L2>(q, rtw_fwd, rtw_inv, 0, 1);
+        else
+            conv_multiply<L1, L2>(q, rtw_fwd, rtw_inv, (unsigned)index, kRaggedMulChunks);
         return;
     }
     const TileArgs a = multi_args<L1, L2>(q, tw, phase);
-    static_assert(C1 >= 1 && C2 >= 1, "tiles of 256 threads");
-    if (phase == 0)
-        tile_body<L1, 16, C1, 1, ACROSS, ACROSS, false>(a, index, 0, 0, 0, smem);
-    else if (phase == 4)
-        tile_body<L1, 16, C1, 1, ACROSS, ACROSS, true>(a, index, 0, 0, 0, smem);
-    else if (phase == 1 && q.stereo)
-        tile_body<L2, 16, C2, 1, ALONG, ALONG, true, false, false, false, true>(a, index, 0, 0, 0, smem);
-    else
-        tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(a, index, 0, 0, 0, smem);
-    __syncthreads();
+    if (phase == 0 || phase == 4) {
+        const int t0 = index < 0 ? 0 : index, t1 = index < 0 ? L2 / C1 : index + 1;
+        for (int t = t0; t < t1; t++) {
+            if (phase == 0)
+                tile_body<L1, 16, C1, 1, ACROSS, ACROSS, false>(a, t, 0, 0, 0, smem);
+            else
+                tile_body<L1, 16, C1, 1, ACROSS, ACROSS, true>(a, t, 0, 0, 0, smem);
+            __syncthreads();
+        }
+    } else {
+        const int t0 = index < 0 ? 0 : index, t1 = index < 0 ? L1 / C2 : index + 1;
+        for (int t = t0; t < t1; t++) {
+            tile_body<L2, 16, C2, 1, ALONG, ALONG, true>(a, t, 0, 0, 0, smem);
+            __syncthreads();
+        }
+    }
+}
+
+// Whole request through the in-CTA four-step.
+template <int L1, int L2>
+__device__ void conv_multi(const RaggedReq &q, float2 *smem, const float2 *tw, const float2 *rtw_fwd,
+                           const float2 *rtw_inv)
+{
+    for (int phase = 0; phase < 5; phase++) {
+        multi_phase<L1, L2>(q, smem, tw, rtw_fwd, rtw_inv, phase, -1);
+        __syncthreads();
+    }
 }
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
@@ -241,26 +274,21 @@ __device__ bool wait_tasks(const unsigned *ctr, unsigned target, int *err)
 
 }  // namespace
 
-namespace {
-
-__host__ __device__ unsigned phase_tasks(unsigned lg, unsigned phase, unsigned stereo)
+unsigned ragged_phase_tasks(unsigned lg, unsigned phase)
 {
-    const unsigned l1 = cr_l1(lg), l2 = cr_l2(lg);
+    // four-step split L1 x L2 of the in-CTA path: 2^14 = 128 x 128, 2^15 = 128 x 256, 2^16 = 256 x 256
+    const unsigned l1 = lg == 16 ? 256 : 128, l2 = lg == 14 ? 128 : 256;
     const unsigned c1 = kThreads * 16 / l1, c2 = kThreads * 16 / l2;
     switch (phase) {
     case 0:
     case 4: return l2 / c1;
     case 1:
     case 3: return l1 / c2;
-    default: return stereo ? 0 : kRaggedMulChunks;  // stereo: the multiply rides in F2
+    default: return kRaggedMulChunks;
     }
 }
 
-}  // namespace
-
-unsigned ragged_phase_tasks(unsigned lg, unsigned phase, unsigned stereo) { return phase_tasks(lg, phase, stereo); }
-
-__global__ void __launch_bounds__(kThreads, 4) conv_ragged_kernel(const RaggedArgs args)
+__global__ void __launch_bounds__(kThreads, 1) conv_ragged_kernel(const RaggedArgs args)
 {
     extern __shared__ float2 smem[];
     __shared__ unsigned s_idx;
@@ -276,6 +304,21 @@ __global__ void __launch_bounds__(kThreads, 4) conv_ragged_kernel(const RaggedAr
         const RaggedReq q = args.reqs[task.req];
         const float2 *rf = args.rtw + args.rtw_off[q.lg];
         const float2 *ri = rf + (1u << q.lg);
+        if (q.split) {
+            if (task.wait && !wait_tasks(&args.counters[q.counter], task.wait, args.err))
+                return;
+            switch (q.lg) {
+            case 14: multi_phase<128, 128>(q, smem, args.tw, rf, ri, task.phase, task.index); break;
+            case 15: multi_phase<128, 256>(q, smem, args.tw, rf, ri, task.phase, task.index); break;
+            case 16: multi_phase<256, 256>(q, smem, args.tw, rf, ri, task.phase, task.index); break;
+            default: break;
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+                atomicAdd(&args.counters[q.counter], 1u);
+            continue;
+        }
         if (task.phase == kRaggedGroupTask) {
             const float2 *const *tab = args.tab + task.pad;
             switch (q.lg) {
@@ -292,52 +335,51 @@ __global__ void __launch_bounds__(kThreads, 4) conv_ragged_kernel(const RaggedAr
             }
             continue;
         }
-        if (task.wait && !wait_tasks(&args.counters[q.counter], task.wait, args.err))
-            return;
-        // one tile / chunk, or (below the split size) all of the phase's in turn
-        int t0 = task.index, t1 = t0 + 1;
-        if (task.index == kRaggedWholePhase) {
-            t0 = 0;
-            t1 = (int)phase_tasks(q.lg, task.phase, q.stereo);
+        // whole requests up to 4096 points always come as group tasks (above)
+        switch (q.lg) {
+        case 13: conv_single<8192>(q, smem, args.tw, rf, ri); break;
+        case 14: conv_single<16384>(q, smem, args.tw, rf, ri); break;
+        case 15: conv_multi<128, 256>(q, smem, args.tw, rf, ri); break;
+        case 16: conv_multi<256, 256>(q, smem, args.tw, rf, ri); break;
+        default: break;
         }
-#pragma unroll 1
-        for (int t = t0; t < t1; t++) {
-            switch (q.lg) {
-            case 13: multi_phase<64, 128>(q, smem, args.tw, rf, ri, task.phase, t); break;
-            case 14: multi_phase<128, 128>(q, smem, args.tw, rf, ri, task.phase, t); break;
-            case 15: multi_phase<128, 256>(q, smem, args.tw, rf, ri, task.phase, t); break;
-            case 16: multi_phase<256, 256>(q, smem, args.tw, rf, ri, task.phase, t); break;
-            default: break;
-            }
-        }
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0)
-            atomicAdd(&args.counters[q.counter], 1u);
     }
 }
 
-unsigned ragged_group_size(unsigned lg) { return lg >= 4 && lg <= kRaggedMaxGroupLg ? (4096u >> lg) : 1u; }
-
-namespace {
-
-template <int L> constexpr size_t group_bytes() { return tile_smem_bytes<L, 16, grp_c<L>(), 1, ALONG, ALONG>(); }
-template <int L1, int L2> constexpr size_t multi_bytes()
+unsigned ragged_group_size(unsigned lg)
 {
-    constexpr size_t a = tile_smem_bytes<L1, 16, kThreads * 16 / L1, 1, ACROSS, ACROSS>();
-    constexpr size_t b = tile_smem_bytes<L2, 16, kThreads * 16 / L2, 1, ALONG, ALONG>();
-    return a > b ? a : b;
+    switch (lg) {
+    case 4: return single_c<16>();
+    case 5: return single_c<32>();
+    case 6: return single_c<64>();
+    case 7: return single_c<128>();
+    case 8: return single_c<256>();
+    case 9: return single_c<512>();
+    case 10: return single_c<1024>();
+    case 11: return single_c<2048>();
+    case 12: return single_c<4096>();
+    default: return 1;
+    }
 }
 
-}  // namespace
+template <int L> constexpr size_t single_bytes()
+{
+    return tile_exchange_bytes<L, single_r<L>(), single_c<L>(), 1, ALONG, ALONG>();
+}
+template <int L1, int L2> constexpr size_t multi_bytes()
+{
+    constexpr size_t a = tile_exchange_bytes<L1, 16, kThreads * 16 / L1, 1, ACROSS, ACROSS>();
+    constexpr size_t b = tile_exchange_bytes<L2, 16, kThreads * 16 / L2, 1, ALONG, ALONG>();
+    return a > b ? a : b;
+}
 
 size_t conv_ragged_smem()
 {
     // every tile conv_ragged_kernel instantiates
-    const size_t v[] = {group_bytes<16>(),   group_bytes<32>(),   group_bytes<64>(),    group_bytes<128>(),
-                        group_bytes<256>(),  group_bytes<512>(),  group_bytes<1024>(),  group_bytes<2048>(),
-                        group_bytes<4096>(), multi_bytes<64, 128>(), multi_bytes<128, 128>(),
-                        multi_bytes<128, 256>(), multi_bytes<256, 256>()};
+    const size_t v[] = {single_bytes<16>(),   single_bytes<32>(),   single_bytes<64>(),   single_bytes<128>(),
+                        single_bytes<256>(),  single_bytes<512>(),  single_bytes<1024>(), single_bytes<2048>(),
+                        single_bytes<4096>(), single_bytes<8192>(), single_bytes<16384>(),
+                        multi_bytes<128, 128>(), multi_bytes<128, 256>(), multi_bytes<256, 256>()};
     size_t m = 0;
     for (size_t x : v)
         m = x > m ? x : m;

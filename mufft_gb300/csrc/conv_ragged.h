@@ -17,8 +17,8 @@ struct RaggedReq {
     unsigned lg;          // log2 of the complex FFT length L (mono N/2, stereo N)
     unsigned stereo;
     unsigned zero_pad;    // first block zero-padded (upper half not read)
-    unsigned split;       // four-step requests: 1 one task per tile / chunk of a phase, 0 one task per phase
-    unsigned counter;     // four-step requests: index of its completion counter
+    unsigned split;       // 1: runs as phase tasks (four-step over several CTAs)
+    unsigned counter;     // split requests: index of its completion counter
 };
 
 // Work item: a whole request, or one task of a phase of a split request.
@@ -32,22 +32,16 @@ struct RaggedTask {
 };
 
 // A group task runs up to C whole requests of one (size, method, zero-pad)
-// class as the C transforms of one tile pair (C = 4096 / L for complex
-// lengths L <= 4096); `req` is its first member.  Its tables in
-// RaggedArgs::tab: count input, filter-spectrum, output and spectrum-scratch
-// pointers, in that order.
+// class as the C transforms of one tile pair (C = the tile's transforms for
+// that size); `req` is its first member.  Its tables in RaggedArgs::tab: count
+// input, filter-spectrum, output and spectrum-scratch pointers, in that order.
 constexpr unsigned short kRaggedGroupTask = 8;
-constexpr unsigned kRaggedMaxGroupLg = 12;
-unsigned ragged_group_size(unsigned lg);  // members per group task
+unsigned ragged_group_size(unsigned lg);  // members per group task (1: whole requests run alone)
 
-// Phase task counts of a four-step request of length 2^lg (L1 x L2); the
-// multiply phase of a stereo request is fused into its row phase (0 tasks).
+// Phase task counts of a split request of length 2^lg (four-step L1 x L2).
 constexpr unsigned kRaggedMulChunks = 8;
-unsigned ragged_phase_tasks(unsigned lg, unsigned phase, unsigned stereo);
-// RaggedTask::index of a task that runs a whole phase of its request.
-constexpr unsigned short kRaggedWholePhase = 0xFFFF;
-constexpr unsigned kRaggedMinSplitLg = 13;  // four-step requests have L >= 8192
-constexpr unsigned kRaggedMinClassLg = 14;  // class pipelines: L >= 16384
+unsigned ragged_phase_tasks(unsigned lg, unsigned phase);
+constexpr unsigned kRaggedMinSplitLg = 14;  // split requests have L >= 16384
 
 struct RaggedArgs {
     const RaggedReq *reqs;

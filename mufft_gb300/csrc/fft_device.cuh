@@ -687,14 +687,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         load_stage0_sin<L, R, C>(a, sin, tile0 + c, c, tl, v);
     } else if constexpr (C2RS) {
         static_assert(LMAP == ALONG && Q == 1 && NST > 1, "staged c2r rows need a row tile with an exchange");
-        if constexpr (TAB) {
-            const unsigned t = tile0 + c;
-            const bool ok = t < a.ntrans;
-            load_stage0_c2r_rows<L, R, COH>(a, ok ? a.in_tab[t] : in, (ok && a.in2_tab) ? a.in2_tab[t] : in2, t, tl,
-                                            smem + c * RS, v);
-        } else {
-            load_stage0_c2r_rows<L, R, COH>(a, in, in2, tile0 + c, tl, smem + c * RS, v);
-        }
+        load_stage0_c2r_rows<L, R, COH>(a, in, in2, tile0 + c, tl, smem + c * RS, v);
         __syncthreads();  // the exchange slices are free again
     } else if constexpr (TAB) {
         const unsigned t = tile0 + c;

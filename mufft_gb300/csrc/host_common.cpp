@@ -158,7 +158,7 @@ bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
         return false;
     }
     *o = *in;
-    auto pow2_range = [](unsigned v, unsigned lo) { return v == 0 || (is_pow2(v) && v >= lo && v <= 65536); };
+    auto pow2_range = [](unsigned v) { return v == 0 || (is_pow2(v) && v >= 16384 && v <= 65536); };
     const char *bad = nullptr;
     if (o->multipass_levels != 0 && o->multipass_levels != 2 && o->multipass_levels != 3)
         bad = "multipass_levels must be 0 (automatic), 2 or 3";
@@ -176,8 +176,8 @@ bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
         bad = "split_engine must be 0 (tcgen05) or 1 (mma.sync)";
     else if (o->columns_2d < 0 || o->columns_2d > 2)
         bad = "columns_2d must be 0 (automatic), 1 (one pass) or 2 (two passes)";
-    else if (!pow2_range(o->conv_split, 8192) || !pow2_range(o->conv_classes, 16384))
-        bad = "conv_split must be 0 or a power of two in 8192..65536, conv_classes 0 or one in 16384..65536";
+    else if (!pow2_range(o->conv_split) || !pow2_range(o->conv_classes))
+        bad = "conv_split and conv_classes must be 0 or powers of two in 16384..65536";
     else if (o->stream_conv_ranges > (1u << 20))
         bad = "at most 2^20 partition ranges";
     else if (o->stream_conv_fused < 0 || o->stream_conv_fused > 1)

@@ -183,7 +183,7 @@ def test_conv_batch_autotuned_split_size(gpu, ora, torch):
     bt = Batch(gpu, torch, specs, 94000, flags=K.FLAG_AUTOTUNE)
     try:
         split = gpu.gb_conv_batch_split_size(bt.handle)
-        assert split in (0, 1 << 13, 1 << 14, 1 << 15, 1 << 16)
+        assert split in (0, 1 << 14, 1 << 15, 1 << 16)
         assert gpu.gb_conv_batch_class_size(bt.handle) in (0, 1 << 14, 1 << 15, 1 << 16)
         outs = bt.run(torch)
     finally:
@@ -193,7 +193,7 @@ def test_conv_batch_autotuned_split_size(gpu, ora, torch):
         assert rel_l2(got, want) <= REL_L2_TOL, (i, N, method, split)
 
 
-@pytest.mark.parametrize("split", [0, 1 << 13, 1 << 14, 1 << 15])
+@pytest.mark.parametrize("split", [0, 1 << 14, 1 << 15])
 def test_conv_batch_forced_split_sizes(gpu, ora, torch, split):
     """Every split size gives the oracle's outputs (phase tasks with their
     bounded dependency waits, or whole requests)."""
