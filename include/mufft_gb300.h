@@ -106,9 +106,6 @@ typedef struct mufft_gb_options {
     /* 2D columns: 0 automatic (8192 points and more as a two-pass four-step
      * of short, wide column tiles), 1 one pass, 2 two passes where possible */
     int columns_2d;
-    /* column passes as persistent CTAs that prefetch their next tile into L2
-     * (1) or one CTA per tile (0) */
-    int prefetch_columns;
     /* ragged convolution batches: requests of at least conv_split complex
      * points run as phase tasks over many CTAs (0: none), of at least
      * conv_classes points as class pipelines (0: none); powers of two in

@@ -63,7 +63,6 @@ struct DeviceGuard {
 const std::vector<TileKernel> &tile_table();
 const TmaTileKernel *find_tma(int L, int R, int C, int nbuf);
 const StreamTileKernel *find_stream(int L, int R, int C);
-const StreamTileKernel *find_prefetch(int L, int R, int C);
 
 // ----------------------------------------------------------------- options
 
@@ -72,8 +71,7 @@ const StreamTileKernel *find_prefetch(int L, int R, int C);
 // field at its built-in default; `tiles` are preferred (L, lmap, smap) ->
 // (C, R, Q).
 struct PlanOptions {
-    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2,
-        prefetch = -2;
+    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2;
     std::vector<TileKernel> tiles;
 };
 // The options of the plan being built on this thread (null: defaults).
@@ -99,7 +97,6 @@ int opt_occ();
 int opt_stream();
 int opt_split_engine();
 int opt_cols2d();
-int opt_prefetch();
 
 // ------------------------------------------------------------ device state
 
@@ -152,9 +149,6 @@ struct Pass {
     // `k` is the same tile as one launch per tile
     const StreamTileKernel *sk = nullptr;
     unsigned sk_grid = 0;
-    // column tiles as persistent CTAs prefetching their next tile into L2
-    // (tiles_prefetch.cu), same launch form as `sk`
-    bool sk_prefetch = false;
 };
 
 struct Buffers {
@@ -204,7 +198,6 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
 bool attach_tma(std::vector<Pass> &ps, PlanResources &res, bool dry, int device);
 bool attach_stream(std::vector<Pass> &ps, bool dry, int device);
 bool attach_occupancy(std::vector<Pass> &ps, bool dry, int device);
-bool attach_prefetch(std::vector<Pass> &ps, bool dry, int device);
 
 // Lazily allocated device staging for host-memory arguments.
 struct Staging {

@@ -194,7 +194,7 @@ std::string describe(const std::vector<Pass> &ps)
         const Pass &p = ps[i];
         if (p.type == PASS_TILE)
             snprintf(buf, sizeof(buf), "%stile%s L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s%s conj=%d",
-                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? (p.sk_prefetch ? "+pf" : "+stream") : ""), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
+                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? "+stream" : ""), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.sk ? p.sk_grid : p.grid.x, p.grid.y, p.k->threads, std::max(p.k->smem, p.smem_min),
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
                      p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
@@ -343,38 +343,6 @@ bool attach_stream(std::vector<Pass> &ps, bool dry, int device)
                 return false;
         }
         p.sk = sk;
-        p.sk_grid = std::min(p.grid.x, (unsigned)(sms * std::max(per_sm, 1)));
-    }
-    return true;
-}
-
-// Gives every column-tile pass (one grid row, unit column distance) that has
-// an L2-prefetching persistent variant that variant: SMs x resident CTAs,
-// each looping over tiles and prefetching the rows of its next one.
-bool attach_prefetch(std::vector<Pass> &ps, bool dry, int device)
-{
-    if (opt_prefetch() != 1)
-        return true;
-    for (Pass &p : ps) {
-        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.k->lmap != ACROSS || p.k->smap != ACROSS || p.tk ||
-            p.sk || p.grid.y != 1 || p.a.ysplit || p.a.in_dist != 1 || p.a.in_stride <= 0)
-            continue;
-        const StreamTileKernel *pk = find_prefetch(p.k->L, p.k->R, p.k->C);
-        if (!pk)
-            continue;
-        int sms = 152, per_sm = 1;
-        if (!dry) {
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-            if (pk->smem > 48 * 1024 &&
-                !cuda_ok(cudaFuncSetAttribute(pk->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pk->smem),
-                         "cudaFuncSetAttribute(prefetch)"))
-                return false;
-            if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pk->fn, pk->threads, pk->smem),
-                         "occupancy(prefetch)"))
-                return false;
-        }
-        p.sk = pk;
-        p.sk_prefetch = true;
         p.sk_grid = std::min(p.grid.x, (unsigned)(sms * std::max(per_sm, 1)));
     }
     return true;

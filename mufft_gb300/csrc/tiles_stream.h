@@ -16,8 +16,5 @@ struct StreamTileKernel {
 };
 
 void register_tiles_stream(std::vector<StreamTileKernel> &out);
-// Persistent column tiles (ACROSS / ACROSS) prefetching their next tile into
-// L2 (tiles_prefetch.cu), same kernel signature.
-void register_tiles_prefetch(std::vector<StreamTileKernel> &out);
 
 }  // namespace mgb

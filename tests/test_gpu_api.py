@@ -284,41 +284,3 @@ def test_tile_occupancy_cap(gpu, torch, occ):
     assert not gpu.gb_create_plan_1d(0, 1024, K.FORWARD, 0, 1, 0, 0, C.byref(bad))
     assert gpu.gb_last_error() == -1
     gpu.gb_clear_error()
-
-
-@pytest.mark.parametrize("N,B", [(1 << 17, 1), (1 << 21, 1), (1 << 24, 1)])
-def test_prefetching_column_tiles(gpu, torch, N, B):
-    """Column passes as persistent CTAs that prefetch their next tile into L2
-    (option prefetch_columns) against FP64, both directions; and the 2D
-    4096-point columns."""
-    x = signals.complex_uniform(29000 + N, N * B).reshape(B, N)
-    dx = _dev(torch, x)
-    dy = torch.empty_like(dx)
-    opts = gpu.options(prefetch_columns=1)
-    for direction in (K.FORWARD, K.INVERSE):
-        plan = gpu.gb_create_plan_1d(0, N, direction, 0, B, 0, 0, C.byref(opts))
-        assert plan, gpu.gb_last_error_string()
-        buf = C.create_string_buffer(4096)
-        gpu.gb_plan_1d_describe(plan, buf, 4096)
-        assert b"+pf" in buf.value, buf.value
-        assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
-        torch.cuda.synchronize()
-        gpu.free_plan_1d(plan)
-        got = dy.cpu().numpy()
-        for r in range(B):
-            ref = np.fft.fft(x[r].astype(np.complex128))
-            if direction == K.INVERSE:
-                ref = np.fft.ifft(x[r].astype(np.complex128)) * N
-            assert rel_l2(got[r], ref) < 2e-6, (r, direction)
-
-
-def test_prefetching_column_tiles_2d(gpu):
-    Nx, Ny = 512, 4096
-    opts = gpu.options(prefetch_columns=1)
-    xr = signals.uniform(29500, Nx * Ny).reshape(Ny, Nx)
-    X = gpu.fft2_r2c(xr, opts=opts)
-    assert rel_l2(X[:, : Nx // 2 + 1], np.fft.rfft2(xr.astype(np.float64))) < 2e-6
-    back = gpu.fft2_c2r(X, opts=opts)
-    assert rel_l2(back / (Nx * Ny), xr) < 4e-6
-    x = signals.complex_uniform(29501, Nx * Ny).reshape(Ny, Nx)
-    assert rel_l2(gpu.fft2_c2c(x, K.FORWARD, opts=opts), np.fft.fft2(x.astype(np.complex128))) < 2e-6
