@@ -160,6 +160,18 @@ int mufft_gb_execute_conv_input_async(mufft_plan_conv *plan, unsigned block, voi
 int mufft_gb_execute_conv_output_async(mufft_plan_conv *plan, void *output, const void *input_first,
                                        const void *input_second, void *stream);
 
+/* `count` executes of a 1D plan on buffers in any memory -- typically page-
+ * locked host memory from mufft_alloc -- with the copies overlapped: input
+ * i + 1 is copied to the device while transform i runs and output i - 1 is
+ * copied back (two device slots of each, made on the plan's first call, and
+ * a copy-in, a compute and a copy-out stream).  Returns when every output is
+ * written, like mufft_execute_plan_1d called `count` times (fft.c:811-850),
+ * which runs one transform's copies and kernels in turn.  Pageable host
+ * memory works but its copies do not overlap.  Not for convolution output
+ * plans.  No counterpart in the reference. */
+int mufft_gb_execute_plan_1d_host_pipeline(mufft_plan_1d *plan, void *const *outputs, const void *const *inputs,
+                                           unsigned count);
+
 /* Enqueue only launches [first, first + count) of a 1D plan's schedule (see
  * mufft_gb_plan_1d_describe), for timing one kernel of a multi-pass plan.
  * Intermediate launches read and write the plan's scratch. */

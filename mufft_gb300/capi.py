@@ -74,6 +74,7 @@ GB_H = [
     ("create_plan_1d_c2r_batched", _vp, [_u, _u, _u, _sz, _sz]),
     ("execute_plan_1d_async", _i, [_vp, _vp, _vp, _vp]),
     ("execute_plan_1d_launches_async", _i, [_vp, _vp, _vp, _u, _u, _vp]),
+    ("execute_plan_1d_host_pipeline", _i, [_vp, _vp, _vp, _u]),
     ("execute_plan_2d_async", _i, [_vp, _vp, _vp, _vp]),
     ("execute_conv_input_async", _i, [_vp, _u, _vp, _vp, _vp]),
     ("execute_conv_output_async", _i, [_vp, _vp, _vp, _vp, _vp]),

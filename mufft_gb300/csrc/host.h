@@ -228,6 +228,16 @@ struct mufft_plan_1d {
     mgb::Staging stage;
     cudaStream_t stream = nullptr;
     bool uses_in2 = false;
+    // pipelined host execution (mufft_gb_execute_plan_1d_host_pipeline): two
+    // device input and output slots, a copy-in, a compute and a copy-out
+    // stream, made on first use
+    struct Pipeline {
+        void *in[2] = {nullptr, nullptr}, *out[2] = {nullptr, nullptr};
+        cudaStream_t st[3] = {nullptr, nullptr, nullptr};
+        cudaEvent_t in_ready[2] = {}, computed[2] = {}, in_free[2] = {}, out_free[2] = {};
+        bool ready = false;
+        void release();
+    } pipe;
 
     size_t in_total() const { return ((size_t)(batch - 1) * idist + in_count) * in_elem; }
     size_t out_total() const { return ((size_t)(batch - 1) * odist + out_count) * out_elem; }

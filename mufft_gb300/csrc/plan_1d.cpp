@@ -13,6 +13,30 @@
 
 namespace mgb {
 
+}  // namespace mgb
+
+void mufft_plan_1d::Pipeline::release()
+{
+    for (int i = 0; i < 2; i++) {
+        cudaFree(in[i]);
+        cudaFree(out[i]);
+        in[i] = out[i] = nullptr;
+        for (cudaEvent_t *e : {&in_ready[i], &computed[i], &in_free[i], &out_free[i]})
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
+    }
+    for (cudaStream_t &s : st)
+        if (s) {
+            cudaStreamDestroy(s);
+            s = nullptr;
+        }
+    ready = false;
+}
+
+namespace mgb {
+
 void destroy_1d(mufft_plan_1d *pl)
 {
     if (!pl)
@@ -21,6 +45,7 @@ void destroy_1d(mufft_plan_1d *pl)
         DeviceGuard g(pl->device);
         pl->res.release();
         pl->stage.release();
+        pl->pipe.release();
         if (pl->stream)
             cudaStreamDestroy(pl->stream);
     }
@@ -567,6 +592,81 @@ int mufft_gb_execute_plan_1d_async(mufft_plan_1d *plan, void *output, const void
         return MUFFT_GB_ERR_INVALID;
     }
     return exec_1d(plan, output, input, nullptr, (cudaStream_t)stream, false);
+}
+
+// Transforms `count` inputs into `count` outputs with the copies of one
+// transform overlapping the kernels and copies of its neighbours: input i + 1
+// is copied in while transform i runs and output i - 1 is copied out.
+int mufft_gb_execute_plan_1d_host_pipeline(mufft_plan_1d *plan, void *const *outputs, const void *const *inputs,
+                                           unsigned count)
+{
+    if (!plan || (count && (!outputs || !inputs))) {
+        set_error(MUFFT_GB_ERR_INVALID, "null plan or buffer lists");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    if (plan->uses_in2) {
+        set_error(MUFFT_GB_ERR_INVALID, "plan needs two inputs");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    for (unsigned i = 0; i < count; i++)
+        if (!outputs[i] || !inputs[i]) {
+            set_error(MUFFT_GB_ERR_INVALID, "null buffer %u", i);
+            return MUFFT_GB_ERR_INVALID;
+        }
+    t_err = 0;
+    DeviceGuard g(plan->device);
+    mufft_plan_1d::Pipeline &P = plan->pipe;
+    const size_t ib = plan->in_total(), ob = plan->out_total();
+    if (!P.ready) {
+        bool ok = true;
+        for (int i = 0; i < 2 && ok; i++)
+            ok = cuda_ok(cudaMalloc(&P.in[i], ib), "cudaMalloc(pipeline)") &&
+                 cuda_ok(cudaMalloc(&P.out[i], ob), "cudaMalloc(pipeline)") &&
+                 cuda_ok(cudaEventCreateWithFlags(&P.in_ready[i], cudaEventDisableTiming), "cudaEventCreate") &&
+                 cuda_ok(cudaEventCreateWithFlags(&P.computed[i], cudaEventDisableTiming), "cudaEventCreate") &&
+                 cuda_ok(cudaEventCreateWithFlags(&P.in_free[i], cudaEventDisableTiming), "cudaEventCreate") &&
+                 cuda_ok(cudaEventCreateWithFlags(&P.out_free[i], cudaEventDisableTiming), "cudaEventCreate");
+        for (int s = 0; s < 3 && ok; s++)
+            ok = cuda_ok(cudaStreamCreateWithFlags(&P.st[s], cudaStreamNonBlocking), "cudaStreamCreate");
+        if (!ok) {
+            P.release();
+            return t_err;
+        }
+        P.ready = true;
+    }
+    cudaStream_t cin = P.st[0], comp = P.st[1], cout = P.st[2];
+    for (unsigned i = 0; i < count; i++) {
+        const int s = (int)(i & 1);
+        // input slot s is free once transform i - 2 has read it; output slot s
+        // once output i - 2 has been copied out
+        if (i >= 2 && !cuda_ok(cudaStreamWaitEvent(cin, P.in_free[s], 0), "pipeline"))
+            return t_err;
+        if (!cuda_ok(cudaMemcpyAsync(P.in[s], inputs[i], ib, cudaMemcpyDefault, cin), "H2D copy") ||
+            !cuda_ok(cudaEventRecord(P.in_ready[s], cin), "pipeline") ||
+            !cuda_ok(cudaStreamWaitEvent(comp, P.in_ready[s], 0), "pipeline") ||
+            (i >= 2 && !cuda_ok(cudaStreamWaitEvent(comp, P.out_free[s], 0), "pipeline")))
+            return t_err;
+        Buffers b{P.in[s], P.out[s], nullptr, plan->res.scratch};
+        if (!cuda_ok(run_passes(plan->passes, b, comp), "kernel launch") ||
+            !cuda_ok(cudaEventRecord(P.in_free[s], comp), "pipeline") ||
+            !cuda_ok(cudaEventRecord(P.computed[s], comp), "pipeline") ||
+            !cuda_ok(cudaStreamWaitEvent(cout, P.computed[s], 0), "pipeline") ||
+            !cuda_ok(cudaMemcpyAsync(outputs[i], P.out[s], ob, cudaMemcpyDefault, cout), "D2H copy") ||
+            !cuda_ok(cudaEventRecord(P.out_free[s], cout), "pipeline"))
+            return t_err;
+    }
+    for (cudaStream_t st : {cin, comp, cout})
+        if (!cuda_ok(cudaStreamSynchronize(st), "execute"))
+            return t_err;
+    if (plan->res.err) {
+        int e = 0;
+        if (cuda_ok(cudaMemcpy(&e, plan->res.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag") && e) {
+            set_error(MUFFT_GB_ERR_UNSUPPORTED, "a bounded wait in a persistent kernel timed out");
+            cudaMemset(plan->res.err, 0, sizeof(int));
+            return t_err;
+        }
+    }
+    return MUFFT_GB_OK;
 }
 
 void mufft_free_plan_1d(mufft_plan_1d *plan) { destroy_1d(plan); }

@@ -299,3 +299,8 @@ def test_fft_batch_validates_requests_on_host(lib):
     assert lib.gb_fft_batch_status(None) == -1
     lib.gb_clear_error()
     lib.gb_free_fft_batch(None)
+
+
+def test_host_pipeline_validates_on_host(lib):
+    assert lib.gb_execute_plan_1d_host_pipeline(None, None, None, 0) == -1
+    lib.gb_clear_error()

@@ -284,3 +284,42 @@ def test_tile_occupancy_cap(gpu, torch, occ):
     assert not gpu.gb_create_plan_1d(0, 1024, K.FORWARD, 0, 1, 0, 0, C.byref(bad))
     assert gpu.gb_last_error() == -1
     gpu.gb_clear_error()
+
+
+@pytest.mark.parametrize("kind,N,B", [(0, 1 << 20, 1), (0, 1024, 64), (1, 1 << 16, 3), (2, 4096, 5)])
+@pytest.mark.parametrize("count", [1, 2, 5])
+def test_host_pipeline_matches_sync_execute(gpu, kind, N, B, count):
+    """mufft_gb_execute_plan_1d_host_pipeline on page-locked and pageable host
+    buffers gives, bit for bit, what mufft_execute_plan_1d gives per buffer."""
+    plan = gpu.gb_create_plan_1d(kind, N, K.FORWARD if kind != 2 else K.INVERSE, 0, B, 0, 0, None)
+    assert plan, gpu.gb_last_error_string()
+    try:
+        if kind == 0:
+            xs = [signals.complex_uniform(29600 + i, N * B) for i in range(count)]
+            nout, dt = N * B, np.complex64
+        elif kind == 1:
+            xs = [signals.uniform(29600 + i, N * B) for i in range(count)]
+            nout, dt = (N // 2 + 1) * B, np.complex64
+        else:
+            xs = [signals.complex_uniform(29600 + i, (N // 2 + 1) * B) for i in range(count)]
+            nout, dt = N * B, np.float32
+        pinned = [gpu.alloc(x.nbytes) for x in xs]
+        for h, x in zip(pinned, xs):
+            C.memmove(h, x.ctypes.data, x.nbytes)
+        outs_p = [gpu.alloc(nout * np.dtype(dt).itemsize) for _ in xs]
+        outs_q = [np.full(nout, np.nan, dt) for _ in xs]  # pageable
+        for outs in (outs_p, [o.ctypes.data for o in outs_q]):
+            ins = (C.c_void_p * count)(*pinned)
+            ol = (C.c_void_p * count)(*outs)
+            assert gpu.gb_execute_plan_1d_host_pipeline(plan, ol, ins, count) == 0, gpu.gb_last_error_string()
+        for i, x in enumerate(xs):
+            want = np.full(nout, np.nan, dt)
+            gpu.execute_plan_1d(plan, want.ctypes.data, pinned[i])
+            gpu.check("execute")
+            got_p = np.frombuffer((C.c_char * want.nbytes).from_address(outs_p[i]), dt)
+            assert np.array_equal(got_p.view(np.uint32), want.view(np.uint32)), i
+            assert np.array_equal(outs_q[i].view(np.uint32), want.view(np.uint32)), i
+        for h in pinned + outs_p:
+            gpu.free(h)
+    finally:
+        gpu.free_plan_1d(plan)
