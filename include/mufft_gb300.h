@@ -91,9 +91,6 @@ typedef struct mufft_gb_options {
     /* inter-pass twiddles: -1 automatic, 0 sincospif per element, 1 FP64
      * table times a per-tile factor, 2 per-tile column powers */
     int twiddle_table;
-    /* the inter-pass twiddle values themselves from an FP64 table of the
-     * pass's modulus (two cached loads and a product, 1) or from sincospif (0) */
-    int twiddle_from_table;
     /* three-level N1 x 65536 transforms: last two passes as one persistent
      * launch with an L2-resident intermediate (1) or two launches (0) */
     int fused_passes;

@@ -152,7 +152,6 @@ MAX_TILE_CHOICES = 8
 class Options(C.Structure):
     """mufft_gb_options (include/mufft_gb300.h): per-plan schedule choices."""
     _fields_ = [("size", C.c_uint), ("multipass_levels", C.c_int), ("twiddle_table", C.c_int),
-                ("twiddle_from_table", C.c_int),
                 ("fused_passes", C.c_int), ("tma", C.c_int), ("tile_occupancy", C.c_int), ("stream_tiles", C.c_int),
                 ("split_engine", C.c_int), ("columns_2d", C.c_int), ("conv_split", C.c_uint),
                 ("conv_classes", C.c_uint), ("stream_conv_ranges", C.c_uint), ("stream_conv_fused", C.c_int),

@@ -103,13 +103,6 @@ struct TileArgs {
     // transform index (column passes of a 2D four-step: W_N^(k*row) for every
     // column of the tile, from a per-CTA table)
     int tw_by_y;
-    // FP64-generated four-step twiddles of this pass's modulus N (or null:
-    // sincospif): [k] = W_N^k for k < 4096, then [4096 + j] = W_N^(4096*j);
-    // W_N^m is the product of the entries of m's high and low 12-bit parts
-    const float2 *tw_tab;
 };
-
-// Entries of a four-step twiddle table for modulus N (a power of two).
-inline unsigned long long fourstep_table_len(unsigned long long N) { return 4096 + (N > 4096 ? N / 4096 : 0); }
 
 }  // namespace mgb

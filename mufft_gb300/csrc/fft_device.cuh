@@ -538,20 +538,6 @@ __device__ __forceinline__ float2 fourstep_twiddle(unsigned m, float scale, unsi
     return cmul(make_float2(c, -s), make_float2(c2, -s2));
 }
 
-// The four-step twiddle of a pass: from its FP64 table when it has one (two
-// cached loads and one product), else from sincospif.
-__device__ __forceinline__ float2 pass_twiddle(const TileArgs &a, unsigned m)
-{
-    if (a.tw_tab) {
-        m &= a.tw_mask;
-        const float2 lo = __ldg(&a.tw_tab[m & 4095u]);
-        if (m < 4096u)
-            return lo;
-        return cmul(__ldg(&a.tw_tab[4096u + (m >> 12)]), lo);
-    }
-    return fourstep_twiddle(m, a.tw_scale, a.tw_mask);
-}
-
 // Real-to-complex fix-up of bin k from Z[k] and Z[M-k] (kernel.c:47-82).
 __device__ __forceinline__ void r2c_bins(float2 zk, float2 zmk, float2 w, float2 &lo, float2 &hi)
 {
@@ -665,7 +651,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         if (a.epilogue == EPI_TWIDDLE && a.tw_by_y) {
             // W_N^(k*row) for every output k, the same for all columns
             for (int k = threadIdx.x; k < L; k += tile_threads<L, R, C, Q>())
-                thi[k] = pass_twiddle(a, (unsigned)k * twy);
+                thi[k] = fourstep_twiddle((unsigned)k * twy, a.tw_scale, a.tw_mask);
             if constexpr (NST == 1)
                 __syncthreads();
         } else if (a.epilogue == EPI_TWIDDLE && a.tw_colpow) {
@@ -675,7 +661,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
             for (int idx = threadIdx.x; idx < C * R; idx += tile_threads<L, R, C, Q>()) {
                 const int cc = idx % C, i = idx / C;  // [i][c]: neighbouring columns in neighbouring banks
                 const unsigned off = (unsigned)(TL * (i / rl) + (i % rl) * BL);
-                thi[idx] = pass_twiddle(a, (tile0 + cc) * off);
+                thi[idx] = fourstep_twiddle((tile0 + cc) * off, a.tw_scale, a.tw_mask);
             }
             if constexpr (NST == 1)
                 __syncthreads();
@@ -683,7 +669,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
             // Four-step twiddle, per-tile half: W_N^(k*C*tile) for every output k
             // (the per-column half W_N^(k*c) comes from the plan's table tw_lo).
             for (int k = threadIdx.x; k < L; k += tile_threads<L, R, C, Q>())
-                thi[k] = pass_twiddle(a, (unsigned)k * (unsigned)(C * tile));
+                thi[k] = fourstep_twiddle((unsigned)k * (unsigned)(C * tile), a.tw_scale, a.tw_mask);
             if constexpr (NST == 1)
                 __syncthreads();
         }
@@ -800,7 +786,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
             float2 wbase = make_float2(1.f, 0.f);
             if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
                 if (a.tw_colpow && !a.tw_by_y)
-                    wbase = pass_twiddle(a, (unsigned)p0 * tr);
+                    wbase = fourstep_twiddle((unsigned)p0 * tr, a.tw_scale, a.tw_mask);
             }
 #pragma unroll
             for (int u = 0; u < NBL; u++)
@@ -817,9 +803,9 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                         else if (a.tw_lo)
                             w = cmul(__ldg(&a.tw_lo[k * C + c]), thi[k]);
                         else
-                            w = pass_twiddle(a, (unsigned)k * tr);
+                            w = fourstep_twiddle((unsigned)k * tr, a.tw_scale, a.tw_mask);
                     } else {
-                        w = pass_twiddle(a, (unsigned)k * (a.tw_by_y ? twy : tr));
+                        w = fourstep_twiddle((unsigned)k * (a.tw_by_y ? twy : tr), a.tw_scale, a.tw_mask);
                     }
                     float2 y = cmul(v[u * rl + m], w);
                     if (a.conj & 2)

@@ -71,8 +71,7 @@ const StreamTileKernel *find_stream(int L, int R, int C);
 // field at its built-in default; `tiles` are preferred (L, lmap, smap) ->
 // (C, R, Q).
 struct PlanOptions {
-    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2,
-        fstab = -2;
+    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2;
     std::vector<TileKernel> tiles;
 };
 // The options of the plan being built on this thread (null: defaults).
@@ -98,7 +97,6 @@ int opt_occ();
 int opt_stream();
 int opt_split_engine();
 int opt_cols2d();
-int opt_fstab();
 
 // ------------------------------------------------------------ device state
 
@@ -144,8 +142,6 @@ struct Pass {
     SplitArgs sp{};
     int sp_stages = 0, sp_limbs = 0, sp_engine = 0;
     unsigned sp_grid = 0;
-    // four-step twiddles from an FP64 table (TileArgs::tw_tab) instead of sincospif
-    bool tw_from_table = false;
     // resident-CTA cap: tile launches request at least this much dynamic
     // shared memory (0: the kernel's own need)
     size_t smem_min = 0;
@@ -195,8 +191,6 @@ struct PlanResources {
     unsigned *afrag = nullptr;    // split precision: DFT-16 limbs in mma fragment order
     float2 *sptw = nullptr;       // split precision: stage twiddles
     void *bfrag = nullptr;        // split precision (tcgen05): DFT-16 limbs as B operands
-    float2 *fstab = nullptr;      // FP64 four-step twiddle table of the first column pass (modulus M)
-    float2 *fstab2 = nullptr;     // three-level: the same for the second column pass
     void release();
 };
 

@@ -146,7 +146,6 @@ int opt_occ() { return opt_field(&PlanOptions::occ, 0); }
 int opt_stream() { return opt_field(&PlanOptions::stream, 0); }
 int opt_split_engine() { return opt_field(&PlanOptions::split_engine, 0); }
 int opt_cols2d() { return opt_field(&PlanOptions::cols2d, 0); }
-int opt_fstab() { return opt_field(&PlanOptions::fstab, 0); }
 
 bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
 {
@@ -175,8 +174,6 @@ bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
         bad = "stream_tiles must be 0 or 1";
     else if (o->split_engine < 0 || o->split_engine > 1)
         bad = "split_engine must be 0 (tcgen05) or 1 (mma.sync)";
-    else if (o->twiddle_from_table < 0 || o->twiddle_from_table > 1)
-        bad = "twiddle_from_table must be 0 or 1";
     else if (o->columns_2d < 0 || o->columns_2d > 2)
         bad = "columns_2d must be 0 (automatic), 1 (one pass) or 2 (two passes)";
     else if (!pow2_range(o->conv_split) || !pow2_range(o->conv_classes))
@@ -210,7 +207,6 @@ bool convert_options(const mufft_gb_options *in, PlanOptions *out)
     p.stream = o.stream_tiles;
     p.split_engine = o.split_engine;
     p.cols2d = o.columns_2d;
-    p.fstab = o.twiddle_from_table;
     for (unsigned i = 0; i < o.ntiles; i++) {
         const mufft_gb_tile_choice &c = o.tiles[i];
         const int lmap = c.load_across ? ACROSS : ALONG, smap = c.store_across ? ACROSS : ALONG;

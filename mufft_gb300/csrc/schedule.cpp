@@ -197,7 +197,7 @@ std::string describe(const std::vector<Pass> &ps)
                      i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? "+stream" : ""), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.sk ? p.sk_grid : p.grid.x, p.grid.y, p.k->threads, std::max(p.k->smem, p.smem_min),
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
-                     p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? (p.tw_from_table ? "/colpow+fstab" : "/colpow") : (p.a.tw_lo ? "/table" : (p.tw_from_table ? "/fstab" : "/sincos"))),
+                     p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
                      p.a.conj);
         else if (p.type == PASS_SPLIT)
             snprintf(buf, sizeof(buf), "%ssplit_tc N=%d bf16x%d %s grid=%u threads=%d smem=%zu conj=%d", i ? "; " : "",
@@ -225,9 +225,6 @@ void PlanResources::release()
     cudaFree(rtw);
     cudaFree(twlo);
     cudaFree(twlo2);
-    cudaFree(fstab);
-    cudaFree(fstab2);
-    fstab = fstab2 = nullptr;
     cudaFree(scratch);
     cudaFree(scratch2);
     cudaFree(ring);
@@ -254,23 +251,6 @@ static bool use_colpow(const TileKernel *k)
 }
 
 // W_M^(k*c) for k < L, c < C: the per-column half of a four-step twiddle.
-// Four-step twiddle table of modulus M (TileArgs::tw_tab): W_M^k for k < 4096,
-// then W_M^(4096*j) for j < M / 4096, FP64 then rounded.
-static bool upload_fstab(unsigned long long M, float2 *&dst)
-{
-    std::vector<float2> t((size_t)fourstep_table_len(M));
-    auto w = [M](unsigned long long m) {
-        const double ph = -2.0 * M_PI * (double)(m % M) / (double)M;
-        return make_float2((float)std::cos(ph), (float)std::sin(ph));
-    };
-    for (unsigned k = 0; k < 4096; k++)
-        t[k] = w(k);
-    for (size_t j = 4096; j < t.size(); j++)
-        t[j] = w(4096ull * (j - 4096));
-    dst = upload(t);
-    return dst != nullptr;
-}
-
 static bool upload_twlo(unsigned L, int C, unsigned long long M, float2 *&dst)
 {
     std::vector<float2> lo((size_t)L * C);
@@ -572,12 +552,8 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
                 (use_twiddle_table(kb) && !upload_twlo(N2, kb->C, MR, res.twlo2)))
                 return false;
             twlo_b = res.twlo2;
-            if (opt_fstab() == 1 && (!upload_fstab(M, res.fstab) || !upload_fstab(MR, res.fstab2)))
-                return false;
         }
         Pass pa = column_pass(ka, tw, N1, (unsigned)MR, (long long)MR, M, res.twlo);
-        pa.a.tw_tab = res.fstab;
-        pa.tw_from_table = opt_fstab() == 1;
         pa.a.in_batch = s.in_dist;
         pa.a.out_batch = M;
         pa.a.conj = s.conj_in ? 1 : 0;
@@ -595,8 +571,6 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
         out.push_back(pa);
 
         Pass pb = column_pass(kb, tw, N2, N3, (long long)N3, MR, twlo_b);
-        pb.a.tw_tab = res.fstab2;
-        pb.tw_from_table = opt_fstab() == 1;
         pb.a.ysplit = N1;
         pb.a.in_batch = pb.a.out_batch = (long long)MR;
         pb.a.in_batch2 = pb.a.out_batch2 = M;
@@ -660,8 +634,6 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
             return false;
         if (use_twiddle_table(kc) && !upload_twlo(N1, kc->C, M, res.twlo))
             return false;
-        if (opt_fstab() == 1 && !upload_fstab(M, res.fstab))
-            return false;
     }
     Pass p1;
     p1.k = kc;
@@ -685,8 +657,6 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p1.a.tw_mask = M - 1;
     p1.a.tw_lo = use_twiddle_table(kc) ? res.twlo : nullptr;
     p1.a.tw_colpow = use_colpow(kc) ? 1 : 0;
-    p1.a.tw_tab = res.fstab;
-    p1.tw_from_table = opt_fstab() == 1;
     p1.in_role = s.in_role;
     p1.in2_role = s.in2_role;
     p1.a.conj2 = s.conj2;

@@ -323,29 +323,3 @@ def test_host_pipeline_matches_sync_execute(gpu, kind, N, B, count):
             gpu.free(h)
     finally:
         gpu.free_plan_1d(plan)
-
-
-@pytest.mark.parametrize("levels", [2, 3])
-@pytest.mark.parametrize("N,B", [(1 << 17, 2), (1 << 20, 3), (1 << 24, 1)])
-def test_fourstep_twiddles_from_tables(gpu, torch, levels, N, B):
-    """Inter-pass twiddles from FP64 tables (option twiddle_from_table)
-    against FP64, both directions."""
-    x = signals.complex_uniform(29700 + N + B, N * B).reshape(B, N)
-    dx = _dev(torch, x)
-    dy = torch.empty_like(dx)
-    opts = gpu.options(multipass_levels=levels, twiddle_from_table=1)
-    for direction in (K.FORWARD, K.INVERSE):
-        plan = gpu.gb_create_plan_1d(0, N, direction, 0, B, 0, 0, C.byref(opts))
-        assert plan, gpu.gb_last_error_string()
-        buf = C.create_string_buffer(4096)
-        gpu.gb_plan_1d_describe(plan, buf, 4096)
-        assert b"fstab" in buf.value, buf.value
-        assert gpu.gb_execute_plan_1d_async(plan, dy.data_ptr(), dx.data_ptr(), _stream(torch)) == 0
-        torch.cuda.synchronize()
-        gpu.free_plan_1d(plan)
-        got = dy.cpu().numpy()
-        for r in range(B):
-            ref = np.fft.fft(x[r].astype(np.complex128))
-            if direction == K.INVERSE:
-                ref = np.fft.ifft(x[r].astype(np.complex128)) * N
-            assert rel_l2(got[r], ref) < 2e-6, (r, direction)
