@@ -646,6 +646,30 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     const unsigned tile0 = tile * C;
 
     static_assert(tile_smem_bytes<L, R, C, Q, LMAP, SMAP>() <= kMaxSmemPerCta, "tile exceeds shared memory");
+    float2 v[R];
+    int c, tl;
+    split_tid<LMAP, C, TL>(threadIdx.x, c, tl);
+    if constexpr (PRE) {
+#pragma unroll
+        for (int q = 0; q < R; q++)
+            v[q] = pre[q];
+    } else if constexpr (SIN) {
+        static_assert(Q == 1 && LMAP == ACROSS, "staged inputs are column tiles");
+        load_stage0_sin<L, R, C>(a, sin, tile0 + c, c, tl, v);
+    } else if constexpr (C2RS) {
+        static_assert(LMAP == ALONG && Q == 1 && NST > 1, "staged c2r rows need a row tile with an exchange");
+        load_stage0_c2r_rows<L, R, COH>(a, in, in2, tile0 + c, tl, smem + c * RS, v);
+        __syncthreads();  // the exchange slices are free again
+    } else if constexpr (TAB) {
+        const unsigned t = tile0 + c;
+        const bool ok = t < a.ntrans;
+        load_stage0<L, R, Q, LMAP, COH>(a, ok ? a.in_tab[t] : in, (ok && a.in2_tab) ? a.in2_tab[t] : in2, t, j, tl,
+                                        v);
+    } else {
+        load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
+    }
+    // The four-step twiddle region is filled while the stage-0 loads are in
+    // flight (the epilogue reads it after the exchanges' barriers).
     if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
         float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
         if (a.epilogue == EPI_TWIDDLE && a.tw_by_y) {
@@ -673,29 +697,6 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
             if constexpr (NST == 1)
                 __syncthreads();
         }
-    }
-
-    float2 v[R];
-    int c, tl;
-    split_tid<LMAP, C, TL>(threadIdx.x, c, tl);
-    if constexpr (PRE) {
-#pragma unroll
-        for (int q = 0; q < R; q++)
-            v[q] = pre[q];
-    } else if constexpr (SIN) {
-        static_assert(Q == 1 && LMAP == ACROSS, "staged inputs are column tiles");
-        load_stage0_sin<L, R, C>(a, sin, tile0 + c, c, tl, v);
-    } else if constexpr (C2RS) {
-        static_assert(LMAP == ALONG && Q == 1 && NST > 1, "staged c2r rows need a row tile with an exchange");
-        load_stage0_c2r_rows<L, R, COH>(a, in, in2, tile0 + c, tl, smem + c * RS, v);
-        __syncthreads();  // the exchange slices are free again
-    } else if constexpr (TAB) {
-        const unsigned t = tile0 + c;
-        const bool ok = t < a.ntrans;
-        load_stage0<L, R, Q, LMAP, COH>(a, ok ? a.in_tab[t] : in, (ok && a.in2_tab) ? a.in2_tab[t] : in2, t, j, tl,
-                                        v);
-    } else {
-        load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
     }
     stage_compute<L, R, Q, 0>(v, j, tl, a.tw);
     run_stages<L, R, C, Q, LMAP, SMAP, 1>(v, j, c, tl, smem, a.tw);
