@@ -668,8 +668,17 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
     } else {
         load_stage0<L, R, Q, LMAP, COH>(a, in, in2, tile0 + c, j, tl, v);
     }
-    // The four-step twiddle region is filled while the stage-0 loads are in
-    // flight (the epilogue reads it after the exchanges' barriers).
+    // The four-step twiddle region, and this thread's column-power base, are
+    // computed while the stage-0 loads are in flight (the epilogue reads the
+    // region after the exchanges' barriers).
+    float2 wbase = make_float2(1.f, 0.f);
+    if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
+        if (a.epilogue == EPI_TWIDDLE && a.tw_colpow && !a.tw_by_y) {
+            int cl, tll;  // the thread's transform and position in the last stage
+            split_tid<SMAP, C, TL>(threadIdx.x, cl, tll);
+            wbase = fourstep_twiddle((unsigned)(j * TT::B(NST - 1) + tll) * (tile0 + cl), a.tw_scale, a.tw_mask);
+        }
+    }
     if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
         float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
         if (a.epilogue == EPI_TWIDDLE && a.tw_by_y) {
@@ -781,14 +790,10 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
         float2 *o0 = out + obase + (long long)p0 * sst;
         if (a.epilogue == EPI_TWIDDLE) {
-            // W_N^(k*n) for output k of column n = tile*C + c.
-            // Twiddle region (filled at kernel start, after the exchange slices)
+            // W_N^(k*n) for output k of column n = tile*C + c: the column-power
+            // base W_N^(p0*n) (wbase) times the region's W_N^(n*off) (filled
+            // while the stage-0 loads were in flight, after the exchange slices)
             float2 *thi = smem + tile_exchange_bytes<L, R, C, Q, LMAP, SMAP>() / sizeof(float2);
-            float2 wbase = make_float2(1.f, 0.f);
-            if constexpr (tile_has_thi<L, R, C, Q, LMAP, SMAP>()) {
-                if (a.tw_colpow && !a.tw_by_y)
-                    wbase = fourstep_twiddle((unsigned)p0 * tr, a.tw_scale, a.tw_mask);
-            }
 #pragma unroll
             for (int u = 0; u < NBL; u++)
 #pragma unroll
