@@ -122,11 +122,16 @@ typedef struct mufft_gb_options {
     /* preferred tile kernels (mufft_gb_list_tiles), first ntiles entries */
     unsigned ntiles;
     mufft_gb_tile_choice tiles[MUFFT_GB_MAX_TILE_CHOICES];
+    /* tile passes as a persistent grid of resident CTAs walking the pass's
+     * tiles wherever the tile has that variant (the 1024-thread 4096-point
+     * column tile): -1 automatic (on), 0 off, 1 on */
+    int persistent_tiles;
 } mufft_gb_options;
 
 /* The defaults: levels 0, twiddles -1, fused 0, tma 0, occupancy 0, stream
  * tiles 0, split engine 0, 2D columns 0, conv_split 65536, conv_classes
- * 16384, stream ranges 0, stream fused 1, fft_split 8192, no tile choices. */
+ * 16384, stream ranges 0, stream fused 1, fft_split 8192, no tile choices,
+ * persistent tiles -1. */
 void mufft_gb_options_init(mufft_gb_options *opts);
 
 /* 1D plans of every kind with options: kind 0 c2c, 1 r2c, 2 c2r (direction

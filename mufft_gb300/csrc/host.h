@@ -29,6 +29,7 @@
 #include "common.h"
 #include "registry.h"
 #include "split_tc.h"
+#include "tiles_persist.h"
 #include "tiles_stream.h"
 #include "tiles_tma.h"
 
@@ -63,6 +64,7 @@ struct DeviceGuard {
 const std::vector<TileKernel> &tile_table();
 const TmaTileKernel *find_tma(int L, int R, int C, int nbuf);
 const StreamTileKernel *find_stream(int L, int R, int C);
+const PersistTileKernel *find_persist(int L, int R, int C, int lmap, int smap);
 
 // ----------------------------------------------------------------- options
 
@@ -71,7 +73,8 @@ const StreamTileKernel *find_stream(int L, int R, int C);
 // field at its built-in default; `tiles` are preferred (L, lmap, smap) ->
 // (C, R, Q).
 struct PlanOptions {
-    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2;
+    int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2,
+        persist = -2;
     std::vector<TileKernel> tiles;
 };
 // The options of the plan being built on this thread (null: defaults).
@@ -97,6 +100,7 @@ int opt_occ();
 int opt_stream();
 int opt_split_engine();
 int opt_cols2d();
+int opt_persist();
 
 // ------------------------------------------------------------ device state
 
@@ -149,6 +153,10 @@ struct Pass {
     // `k` is the same tile as one launch per tile
     const StreamTileKernel *sk = nullptr;
     unsigned sk_grid = 0;
+    // the tiles as a persistent grid (tiles_persist.cu); `k` is the same tile
+    // as one launch per tile
+    const PersistTileKernel *pt = nullptr;
+    unsigned pt_grid = 0;
 };
 
 struct Buffers {
@@ -197,6 +205,7 @@ struct PlanResources {
 bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bool dry, std::vector<Pass> &out);
 bool attach_tma(std::vector<Pass> &ps, PlanResources &res, bool dry, int device);
 bool attach_stream(std::vector<Pass> &ps, bool dry, int device);
+bool attach_persist(std::vector<Pass> &ps, bool dry, int device);
 bool attach_occupancy(std::vector<Pass> &ps, bool dry, int device);
 
 // Lazily allocated device staging for host-memory arguments.

@@ -100,6 +100,24 @@ const StreamTileKernel *find_stream(int L, int R, int C)
     return nullptr;
 }
 
+static const std::vector<PersistTileKernel> &persist_table()
+{
+    static const std::vector<PersistTileKernel> t = [] {
+        std::vector<PersistTileKernel> v;
+        register_tiles_persist(v);
+        return v;
+    }();
+    return t;
+}
+
+const PersistTileKernel *find_persist(int L, int R, int C, int lmap, int smap)
+{
+    for (const PersistTileKernel &k : persist_table())
+        if (k.L == L && k.R == R && k.C == C && k.lmap == lmap && k.smap == smap)
+            return &k;
+    return nullptr;
+}
+
 const TileKernel *find_tile(int L, int lmap, int smap, int C, int R, int Q)
 {
     if (C == 0 && R == 0 && Q == 0 && t_opts) {
@@ -133,7 +151,9 @@ thread_local const PlanOptions *t_opts = nullptr;
 //    per-thread loads at four CTAs per SM (the autotuner still tries them);
 //  - no resident-CTA cap, no streaming row tiles (both measured slower);
 //  - split-precision products on tcgen05.mma;
-//  - 2D columns: two-pass four-step from 8192 points.
+//  - 2D columns: two-pass four-step from 8192 points;
+//  - persistent tile grids wherever the tile has that variant (the
+//    1024-thread 4096-point column tile).
 static int opt_field(int PlanOptions::*f, int def)
 {
     return (t_opts && t_opts->*f != -2) ? t_opts->*f : def;
@@ -146,6 +166,7 @@ int opt_occ() { return opt_field(&PlanOptions::occ, 0); }
 int opt_stream() { return opt_field(&PlanOptions::stream, 0); }
 int opt_split_engine() { return opt_field(&PlanOptions::split_engine, 0); }
 int opt_cols2d() { return opt_field(&PlanOptions::cols2d, 0); }
+int opt_persist() { return opt_field(&PlanOptions::persist, 1); }
 
 bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
 {
@@ -184,6 +205,8 @@ bool public_options(const mufft_gb_options *in, mufft_gb_options *o)
         bad = "stream_conv_fused must be 0 or 1";
     else if (o->fft_split != 0 && (!is_pow2(o->fft_split) || o->fft_split < 8192 || o->fft_split > 65536))
         bad = "fft_split must be 0 or a power of two in 8192..65536";
+    else if (o->persistent_tiles < -1 || o->persistent_tiles > 1)
+        bad = "persistent_tiles must be -1 (automatic), 0 or 1";
     else if (o->ntiles > MUFFT_GB_MAX_TILE_CHOICES)
         bad = "at most MUFFT_GB_MAX_TILE_CHOICES tile choices";
     if (bad) {
@@ -207,6 +230,7 @@ bool convert_options(const mufft_gb_options *in, PlanOptions *out)
     p.stream = o.stream_tiles;
     p.split_engine = o.split_engine;
     p.cols2d = o.columns_2d;
+    p.persist = o.persistent_tiles < 0 ? -2 : o.persistent_tiles;
     for (unsigned i = 0; i < o.ntiles; i++) {
         const mufft_gb_tile_choice &c = o.tiles[i];
         const int lmap = c.load_across ? ACROSS : ALONG, smap = c.store_across ? ACROSS : ALONG;
@@ -346,6 +370,7 @@ void mufft_gb_options_init(mufft_gb_options *o)
     o->stream_conv_ranges = 0;
     o->stream_conv_fused = 1;
     o->fft_split = 8192;
+    o->persistent_tiles = -1;
 }
 
 // ================================================================ memory

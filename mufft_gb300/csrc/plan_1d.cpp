@@ -267,6 +267,7 @@ mufft_plan_1d *create_1d(int kind, unsigned N, int direction, unsigned flags, un
         const bool built = build_fft_passes(s, tw, pl->res, dry, pl->passes) &&
                            attach_tma(pl->passes, pl->res, dry, pl->device) &&
                            attach_stream(pl->passes, dry, pl->device) &&
+                           attach_persist(pl->passes, dry, pl->device) &&
                            attach_occupancy(pl->passes, dry, pl->device);
         t_opts = prev;
         if (!built) {

@@ -251,7 +251,8 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         pl->passes.push_back(row);
         pl->passes.push_back(col);
     }
-    if (!attach_stream(pl->passes, false, pl->device) || !attach_occupancy(pl->passes, false, pl->device)) {
+    if (!attach_stream(pl->passes, false, pl->device) || !attach_persist(pl->passes, false, pl->device) ||
+        !attach_occupancy(pl->passes, false, pl->device)) {
         destroy_2d(pl);
         return nullptr;
     }

@@ -79,6 +79,23 @@ static bool tma_map_for(const Pass &p, const float2 *in, CUtensorMap *map)
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Dynamic shared memory of a tile launch: the four-step twiddle region only
+// where an epilogue reads it, at least the resident-CTA cap's request.
+static size_t tile_launch_smem(const Pass &p)
+{
+    const TileArgs &a = p.a;
+    return std::max((a.tw_lo || a.tw_colpow || a.tw_by_y) ? p.k->smem : p.k->smem_ex, p.smem_min);
+}
+
+// A row tile with a c2r fix-up prologue over whole rows runs as its variant
+// that stages each row in shared memory.
+static bool uses_c2r_rows(const Pass &p)
+{
+    const TileArgs &a = p.a;
+    return p.k->fn_c2r && (a.prologue == PRO_C2R || a.prologue == PRO_MUL_C2R) && a.mirror_ldist == 0 &&
+           a.mirror_len == p.k->L && !a.half && a.in_stride == 1;
+}
+
 cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream_t st, size_t first, size_t count)
 {
     for (size_t i = first; i < ps.size() && i - first < count; i++) {
@@ -104,6 +121,15 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                     continue;
                 }
             }
+            if (p.pt) {
+                unsigned tiles_x = p.grid.x, ntiles = p.grid.x * p.grid.y;
+                void *pargs[] = {&a, &tiles_x, &ntiles};
+                cudaError_t e = cudaLaunchKernel(p.pt->fn, dim3(std::min(ntiles, p.pt_grid)), dim3(p.pt->threads),
+                                                 pargs, tile_launch_smem(p), st);
+                if (e != cudaSuccess)
+                    return e;
+                continue;
+            }
             if (p.sk) {
                 unsigned ntiles = p.grid.x;
                 void *sargs[] = {&a, &ntiles};
@@ -113,8 +139,7 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                 continue;
             }
             void *args[] = {&a};
-            const size_t smem =
-                std::max((a.tw_lo || a.tw_colpow || a.tw_by_y) ? p.k->smem : p.k->smem_ex, p.smem_min);
+            const size_t smem = tile_launch_smem(p);
             cudaError_t e;
             if (p.k->Q > 1) {
                 // one tile per cluster of Q CTAs (distributed shared memory)
@@ -133,9 +158,8 @@ cudaError_t run_passes(const std::vector<Pass> &ps, const Buffers &b, cudaStream
                 e = cudaLaunchKernelExC(&cfg, p.k->fn, args);
             } else {
                 // c2r fix-up rows staged in shared memory where the tile has that variant
-                const bool c2r_rows = p.k->fn_c2r && (a.prologue == PRO_C2R || a.prologue == PRO_MUL_C2R) &&
-                                      a.mirror_ldist == 0 && a.mirror_len == p.k->L && !a.half && a.in_stride == 1;
-                e = cudaLaunchKernel(c2r_rows ? p.k->fn_c2r : p.k->fn, p.grid, dim3(p.k->threads), args, smem, st);
+                e = cudaLaunchKernel(uses_c2r_rows(p) ? p.k->fn_c2r : p.k->fn, p.grid, dim3(p.k->threads), args, smem,
+                                     st);
             }
             if (e != cudaSuccess)
                 return e;
@@ -194,8 +218,8 @@ std::string describe(const std::vector<Pass> &ps)
         const Pass &p = ps[i];
         if (p.type == PASS_TILE)
             snprintf(buf, sizeof(buf), "%stile%s L=%d R=%d C=%d Q=%d %s/%s grid=%ux%u threads=%d smem=%zu pro=%s%s epi=%s%s conj=%d",
-                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? "+stream" : ""), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
-                     p.k->smap ? "across" : "along", p.sk ? p.sk_grid : p.grid.x, p.grid.y, p.k->threads, std::max(p.k->smem, p.smem_min),
+                     i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? "+stream" : (p.pt ? "+persistent" : "")), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
+                     p.k->smap ? "across" : "along", p.sk ? p.sk_grid : (p.pt ? std::min(p.grid.x * p.grid.y, p.pt_grid) : p.grid.x), p.pt ? 1u : p.grid.y, p.k->threads, std::max(p.k->smem, p.smem_min),
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
                      p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
                      p.a.conj);
@@ -348,6 +372,37 @@ bool attach_stream(std::vector<Pass> &ps, bool dry, int device)
     return true;
 }
 
+// Gives every single-CTA tile pass whose tile has a persistent variant that
+// variant: a grid of SMs x resident CTAs walking the pass's tiles (not for
+// c2r row tiles, which stage their rows in tile_fft_c2r_rows).
+bool attach_persist(std::vector<Pass> &ps, bool dry, int device)
+{
+    if (opt_persist() != 1)
+        return true;
+    for (Pass &p : ps) {
+        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.tk || p.sk || p.grid.z > 1 || uses_c2r_rows(p))
+            continue;
+        const PersistTileKernel *pt = find_persist(p.k->L, p.k->R, p.k->C, p.k->lmap, p.k->smap);
+        if (!pt)
+            continue;
+        int sms = 152, per_sm = 1;
+        if (!dry) {
+            const size_t smem = tile_launch_smem(p);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (!cuda_ok(cudaFuncSetAttribute(pt->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "cudaFuncSetAttribute(persist)") ||
+                !cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt->fn, pt->threads, smem),
+                         "occupancy(persist)"))
+                return false;
+            if (per_sm < 1)
+                continue;
+        }
+        p.pt = pt;
+        p.pt_grid = (unsigned)(sms * per_sm);
+    }
+    return true;
+}
+
 // Applies the resident-CTA cap to every single-CTA tile pass: the launch
 // asks for enough dynamic shared memory that at most `occ` CTAs fit per SM.
 bool attach_occupancy(std::vector<Pass> &ps, bool dry, int device)
@@ -366,7 +421,7 @@ bool attach_occupancy(std::vector<Pass> &ps, bool dry, int device)
         return true;
     const size_t want = (size_t)w & ~(size_t)127;
     for (Pass &p : ps) {
-        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.tk || p.sk)
+        if (p.type != PASS_TILE || !p.k || p.k->Q != 1 || p.tk || p.sk || p.pt)
             continue;
         if (want <= p.k->smem)
             continue;

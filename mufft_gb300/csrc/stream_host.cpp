@@ -87,8 +87,24 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
     c->nb = nb;
     c->pitch = pitch;
     c->stereo = stereo;
-    c->fwd = create_1d(stereo ? K_C2C : K_R2C, L, MUFFT_FORWARD, tflags, 1, 0, 0, -1, false, nullptr);
-    c->inv = create_1d(stereo ? K_C2C : K_C2R, L, MUFFT_INVERSE, tflags, 1, 0, 0, -1, false, nullptr);
+    // The one-launch block needs both window transforms as one 256-thread
+    // row tile of 4096 / M transforms (M complex points each): ask for that
+    // tile unless the caller's options choose one.
+    const unsigned M = stereo ? L : L / 2;
+    PlanOptions wopts = opts ? po : PlanOptions();
+    if (o.stream_conv_fused && upols_block_supported((int)M)) {
+        bool chosen = false;
+        for (const TileKernel &k : wopts.tiles)
+            chosen = chosen || (k.L == (int)M && k.lmap == ALONG && k.smap == ALONG);
+        const TileKernel *k = chosen ? nullptr : find_tile((int)M, ALONG, ALONG, 4096 / (int)M, 16, 1);
+        if (k)
+            wopts.tiles.push_back(*k);
+    }
+    {
+        OptionsScope wscope(&wopts);
+        c->fwd = create_1d(stereo ? K_C2C : K_R2C, L, MUFFT_FORWARD, tflags, 1, 0, 0, -1, false, nullptr);
+        c->inv = create_1d(stereo ? K_C2C : K_C2R, L, MUFFT_INVERSE, tflags, 1, 0, 0, -1, false, nullptr);
+    }
     if (!c->fwd || !c->inv) {
         destroy_stream_conv(c);
         return nullptr;
@@ -103,7 +119,6 @@ mufft_gb_stream_conv *mufft_gb_create_stream_conv(unsigned block, unsigned metho
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     const unsigned want_ranges = o.stream_conv_ranges;
     // One launch per block when both transforms are one 256-thread row tile
-    const unsigned M = stereo ? L : L / 2;
     auto row_tile = [M](const mufft_plan_1d *pl) {
         if (pl->passes.size() != 1)
             return false;

@@ -198,8 +198,8 @@ def _sched(lib, N, kind, direction=K.FORWARD, flags=0, batch=1, opts=None):
 
 
 def test_single_pass_schedule(lib):
-    s = _sched(lib, 1024, 0, batch=4096)
-    assert s.count("tile") == 1 and "L=1024" in s and "grid=1024x1" in s
+    s = _sched(lib, 1024, 0, batch=4096)  # one transform per tile
+    assert s.count("tile") == 1 and "L=1024 R=16 C=1 " in s and "grid=4096x1" in s, s
     s = _sched(lib, 4096, 0, K.INVERSE)
     assert "conj=3" in s
     s = _sched(lib, 8192, 1, flags=K.FLAG_ZERO_PAD_UPPER_HALF)
@@ -238,13 +238,22 @@ def test_schedule_options_in_dry_runs(lib):
     s = _sched(lib, 1024, 0, batch=4096, opts=lib.options(stream_tiles=1))
     assert "tile+stream" in s and "grid=152x1" in s, s
     s = _sched(lib, 1024, 0, batch=4096)
-    assert "+stream" not in s and "smem=34816" in s
-    s = _sched(lib, 1024, 0, batch=4096, opts=lib.options(tiles=[(1024, 0, 0, 1, 16, 1)]))
-    assert "L=1024 R=16 C=1 " in s and "grid=4096x1" in s, s
+    assert "+stream" not in s and "smem=8704" in s, s
+    s = _sched(lib, 1024, 0, batch=4096, opts=lib.options(tiles=[(1024, 0, 0, 4, 16, 1)]))
+    assert "L=1024 R=16 C=4 " in s and "grid=1024x1" in s and "smem=34816" in s, s
+    # 4096-point column tiles (one 1024-thread CTA per SM) run as a persistent
+    # grid by default; the other tiles keep one launch per tile
+    s = _sched(lib, 1 << 24, 0, opts=lib.options(multipass_levels=2))
+    first, second = s.split("; ")
+    assert first.startswith("tile+persistent L=4096 R=16 C=4") and "grid=152x1" in first, s
+    assert "+persistent" not in second, s
+    s = _sched(lib, 1 << 24, 0, opts=lib.options(multipass_levels=2, persistent_tiles=0))
+    assert "+persistent" not in s and "grid=1024x1" in s, s
+    assert "+persistent" not in _sched(lib, 1 << 24, 0)
     buf = C.create_string_buffer(64)
     for bad in (dict(tile_occupancy=-1), dict(tile_occupancy=33), dict(stream_tiles=2), dict(stream_conv_fused=3),
                 dict(stream_conv_ranges=1 << 21), dict(conv_split=1000), dict(twiddle_table=3), dict(tma=3),
-                dict(columns_2d=3)):
+                dict(columns_2d=3), dict(persistent_tiles=2), dict(persistent_tiles=-2)):
         o = lib.options(**bad)
         assert lib.gb_describe_schedule_1d(1024, 0, K.FORWARD, 0, 1, C.byref(o), buf, 64) == -1, bad
         lib.gb_clear_error()
@@ -256,8 +265,8 @@ def test_schedule_options_in_dry_runs(lib):
     assert lib.gb_describe_schedule_1d(1024, 0, K.FORWARD, 0, 1, C.byref(o), buf, 64) == -1
     lib.gb_clear_error()
     d = lib.options()
-    assert (d.multipass_levels, d.twiddle_table, d.conv_split, d.conv_classes, d.stream_conv_fused) == \
-        (0, -1, 65536, 16384, 1)
+    assert (d.multipass_levels, d.twiddle_table, d.conv_split, d.conv_classes, d.stream_conv_fused,
+            d.persistent_tiles) == (0, -1, 65536, 16384, 1, -1)
 
 
 def test_batched_convolution_entry_points_validate_on_host(lib):

@@ -211,6 +211,28 @@ def test_large_conv(gpu, ora, N, method):
     assert_close(gpu.conv(a, b, N, method), ora.conv(a, b, N, method), N, elem_tol=4e-6, what=f"conv {N}")
 
 
+@pytest.mark.parametrize("Nx", [64, 2048])
+def test_2d_persistent_columns_match_oracle(gpu, ora, Nx):
+    """4096-point columns run as a persistent grid (default): the same bits as
+    one launch per tile, and the oracle's results, for r2c, c2r and both c2c
+    directions (64 columns: fewer tiles than SMs; 2048: several tiles per CTA)."""
+    Ny = 4096
+    on, off = gpu.options(persistent_tiles=1), gpu.options(persistent_tiles=0)
+    x = signals.uniform(13100 + Nx, Nx * Ny).reshape(Ny, Nx)
+    vx = Nx // 2 + 1
+    a, b = gpu.fft2_r2c(x, opts=on), gpu.fft2_r2c(x, opts=off)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert_close(a[:, :vx], ora.fft2_r2c(x, 0)[:, :vx], Nx * Ny, what=f"2d r2c {Nx}x{Ny}")
+    X = signals.complex_uniform(13200 + Nx, Nx * Ny).reshape(Ny, Nx)
+    a, b = gpu.fft2_c2r(X, opts=on), gpu.fft2_c2r(X, opts=off)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert_close(a, ora.fft2_c2r(X), Nx * Ny, what=f"2d c2r {Nx}x{Ny}")
+    for d in (K.FORWARD, K.INVERSE):
+        a, b = gpu.fft2_c2c(X, d, opts=on), gpu.fft2_c2c(X, d, opts=off)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        assert_close(a, ora.fft2_c2c(X, d), Nx * Ny, what=f"2d c2c {Nx}x{Ny} {d}")
+
+
 def test_2d_4096_round_trip(gpu):
     Nx = Ny = 4096
     x = signals.normal(13000, Nx * Ny).reshape(Ny, Nx)
