@@ -441,7 +441,7 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
 // mirror_ldist 0, mirror_len L, no `half`.  The row is staged once, coalesced, in the transform's exchange
 // slice (padded positions), and both operands are read from there -- one
 // global load per element instead of two.  X[M] (needed by n = 0 only) is
-// loaded directly.  PRO_MUL_C2R multiplies by s * B[n] while staging.  Not
+// loaded into a register of thread 0 beside the staged values.  PRO_MUL_C2R multiplies by s * B[n] while staging.  Not
 // for zero-padded inputs (`half`).  The caller's CTA must not use the slice
 // until the next barrier.
 template <int L, int R, bool COH>
@@ -464,10 +464,15 @@ __device__ __forceinline__ void load_stage0_c2r_rows(const TileArgs &a, const fl
         }
         return xv;
     };
+    // X[M], the mirror of position 0, is loaded with the staged values so
+    // that its latency is not paid after the barrier
+    float2 xm = make_float2(0.f, 0.f);
     if (valid) {
 #pragma unroll
         for (int i = 0; i < R; i++)
             region[padpos(tl + TL * i)] = fetch(tl + TL * i);
+        if (tl == 0)
+            xm = fetch(L);
     }
     __syncthreads();
 #pragma unroll
@@ -481,7 +486,7 @@ __device__ __forceinline__ void load_stage0_c2r_rows(const TileArgs &a, const fl
                 const int local = tl + TL * u + m * B;
                 const float2 xa = region[padpos(local)];
                 // only register 0 of thread 0 is position 0 (its mirror X[M] is not staged)
-                const float2 xb = (u == 0 && m == 0 && tl == 0) ? fetch(L) : region[padpos(L - local)];
+                const float2 xb = (u == 0 && m == 0 && tl == 0) ? xm : region[padpos(L - local)];
                 v[u * r + m] = c2r_fixup(xa, xb, __ldg(&a.rtw[local]));
             }
     }
@@ -746,7 +751,37 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     dst[padpos(pos - owner * LQ)] = v[u * rl + m];
                 }
             tile_sync<Q>();
-            if (valid) {
+            if (Q == 1 && valid) {
+                // Bins in pairs: Z[k] and Z[M-k] give X[k] = lo and, by the
+                // symmetry of a real input's spectrum, X[M-k] = conj(hi) (and
+                // X[M+k] = hi, X[2M-k] = conj(lo) for the full output), so a
+                // thread resolves k < M/2 and reads each value once.
+                const long long os = a.out_stride;
+#pragma unroll
+                for (int q = 0; q < R / 2; q++) {
+                    const int k = tl + TL * q;
+                    const float2 zk = region[padpos(k)];
+                    if (k == 0) {
+                        out[obase] = make_float2(zk.x + zk.y, 0.f);
+                        out[obase + (long long)M * os] = make_float2(zk.x - zk.y, 0.f);
+                        const float2 zh = region[padpos(M / 2)];  // the middle bin pairs with itself
+                        float2 lo, hi;
+                        r2c_bins(zh, zh, __ldg(&a.rtw[M / 2]), lo, hi);
+                        out[obase + (long long)(M / 2) * os] = lo;
+                        if (full)
+                            out[obase + (long long)(M / 2 + M) * os] = hi;
+                    } else {
+                        float2 lo, hi;
+                        r2c_bins(zk, region[padpos(M - k)], __ldg(&a.rtw[k]), lo, hi);
+                        out[obase + (long long)k * os] = lo;
+                        out[obase + (long long)(M - k) * os] = cconj(hi);
+                        if (full) {
+                            out[obase + (long long)(k + M) * os] = hi;
+                            out[obase + (long long)(2 * M - k) * os] = cconj(lo);
+                        }
+                    }
+                }
+            } else if (valid) {
 #pragma unroll
                 for (int q = 0; q < R; q++) {
                     const int kl = tl + TL * q;  // local position in this CTA's slice
