@@ -383,13 +383,8 @@ mufft_gb_conv_batch *mufft_gb_create_conv_batch(const mufft_gb_conv_request *req
     b->smem = conv_ragged_smem();
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const ClassTile mul128 = class_row_mul_tile(128), mul256 = class_row_mul_tile(256);
     if (!cuda_ok(cudaFuncSetAttribute(conv_ragged_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem),
                  "cudaFuncSetAttribute") ||
-        !cuda_ok(cudaFuncSetAttribute(mul128.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mul128.smem),
-                 "cudaFuncSetAttribute(class multiply rows)") ||
-        !cuda_ok(cudaFuncSetAttribute(mul256.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mul256.smem),
-                 "cudaFuncSetAttribute(class multiply rows)") ||
         !cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_ragged_fn(), conv_ragged_threads(),
                                                                b->smem),
                  "occupancy") ||

@@ -405,19 +405,7 @@ __global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L
 // Phase 1 of a stereo class with the spectral multiply fused into its
 // epilogue: rows k1 of X^T[k1][k2] = X[k1 + L1*k2], times s * H[k1 + L1*k2]
 // (the template's in2_dist = 1, in2_stride = L1); the multiply launch is
-// skipped.  The tile's rows read H's neighbouring elements: the CTA copies
-// its C x L factors into shared memory first (cp.async, C consecutive
-// elements per k2, so whole 128-byte segments), and they arrive while the
-// rows are transformed instead of after.  Measured on the 512-request mix:
-// 97.8 -> 95.9 us per batch (with the factors read in the epilogue instead,
-// straight from HBM at a stride of L1 elements per lane; half-width tiles
-// 97.7 us; the transposed store map, whose factor reads are whole segments,
-// 99.3 us).
-template <int L, int C> __host__ __device__ constexpr size_t class_mul_smem()
-{
-    return tile_smem_bytes<L, 16, C, 1, ALONG, ALONG>() + (size_t)L * (C + 1) * sizeof(float2);
-}
-
+// skipped.  Neighbouring rows of a tile read H's neighbouring elements.
 template <int L, int C>
 __global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L, 16, C, 1>())
     class_tile_mul(const TileArgs tmpl, const ClassEntry *tab, int phase)
@@ -429,19 +417,7 @@ __global__ void __launch_bounds__(tile_threads<L, 16, C, 1>(), tile_min_blocks<L
     a.out = e.spec;
     a.in2 = e.h;
     (void)phase;
-    float2 *hs = smem + tile_smem_bytes<L, 16, C, 1, ALONG, ALONG>() / sizeof(float2);
-    for (int i = threadIdx.x; i < L * C; i += tile_threads<L, 16, C, 1>()) {
-        const int c = i % C, k = i / C;
-        const unsigned tr = blockIdx.x * C + c;
-        if (tr < a.ntrans) {
-            const unsigned d = (unsigned)__cvta_generic_to_shared(&hs[k * (C + 1) + c]);
-            const float2 *src = a.in2 + (long long)tr * a.in2_dist + (long long)k * a.in2_stride;
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
-        }
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    tile_body<L, 16, C, 1, ALONG, ALONG, false, false, false, false, true>(a, blockIdx.x, 0, 0, 0, smem, nullptr, 0,
-                                                                           nullptr, hs);
+    tile_body<L, 16, C, 1, ALONG, ALONG, false, false, false, false, true>(a, blockIdx.x, 0, 0, 0, smem);
 }
 
 // The multiply phase of a mono class (stereo classes fuse it into F2), on the
@@ -528,9 +504,9 @@ ClassTile class_row_mul_tile(int L2)
 {
     if (L2 == 128)
         return ClassTile{(const void *)&class_tile_mul<128, 32>, 128, 32, tile_threads<128, 16, 32, 1>(),
-                         class_mul_smem<128, 32>()};
+                         tile_smem_bytes<128, 16, 32, 1, ALONG, ALONG>()};
     return ClassTile{(const void *)&class_tile_mul<256, 16>, 256, 16, tile_threads<256, 16, 16, 1>(),
-                     class_mul_smem<256, 16>()};
+                     tile_smem_bytes<256, 16, 16, 1, ALONG, ALONG>()};
 }
 
 const void *class_multiply_fn() { return (const void *)&class_multiply; }

@@ -628,17 +628,14 @@ template <int L, int R, int C, int Q> __host__ __device__ constexpr int tile_min
 // C2RS: c2r fix-up prologue through a row staged in shared memory (row
 // tiles; the caller checked load_stage0_c2r_rows's conditions).
 // EMUL: plain epilogue multiplied by scale * in2[tr*in2_dist + k*in2_stride]
-// (the spectral multiply of a convolution, fused into the forward pass); with
-// `hs` (row tiles) the factors come from shared memory instead, hs[k*(C+1) + c]
-// for output k of the tile's transform c, copied there by the caller's
-// cp.async copies, which every thread waits for before the epilogue.
+// (the spectral multiply of a convolution, fused into the forward pass).
 // TAB: every transform of the tile has its own buffers (in_tab / in2_tab /
 // out_tab, distances 0): a tile of C unrelated requests of one size.
 template <int L, int R, int C, int Q, int LMAP, int SMAP, bool COH, bool SIN = false, bool PRE = false,
           bool C2RS = false, bool EMUL = false, bool TAB = false>
 __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int j, long long ioff, long long ooff,
                                           float2 *smem, const float2 *sin = nullptr, unsigned twy = 0,
-                                          const float2 *pre = nullptr, const float2 *hs = nullptr)
+                                          const float2 *pre = nullptr)
 {
     using S = Sched<L, R>;
     using TT = Tile<L, R, Q>;
@@ -824,12 +821,6 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         return;
     }
 
-    if constexpr (EMUL) {
-        if (hs) {  // (uniform over the CTA)
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-            __syncthreads();
-        }
-    }
     if (valid) {
         const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
         float2 *o0 = out + obase + (long long)p0 * sst;
@@ -870,11 +861,9 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                 for (int m = 0; m < rl; m++) {
                     const int off = TL * u + m * Q * BL;
                     float2 y = v[u * rl + m];
-                    if constexpr (EMUL) {
-                        const float2 h = hs ? hs[(p0 + off) * (C + 1) + c]
-                                            : __ldg(&a.in2[(long long)tr * a.in2_dist + (long long)(p0 + off) * a.in2_stride]);
-                        y = cscale(cmul(y, h), a.scale);
-                    }
+                    if constexpr (EMUL)
+                        y = cscale(cmul(y, __ldg(&a.in2[(long long)tr * a.in2_dist + (long long)(p0 + off) * a.in2_stride])),
+                                   a.scale);
                     o0[(long long)off * sst] = make_float2(y.x, sg * y.y);
                 }
         }
