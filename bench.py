@@ -337,13 +337,18 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
         outs_l = (ctypes.c_void_p * e2e_steps)(*[hout[i % 2] for i in range(e2e_steps)])
         assert lib.gb_execute_plan_1d_host_pipeline(hplan, outs_l, ins_l, e2e_steps) == 0  # warm (device slots)
         lib.execute_plan_1d(hplan, hout[0], hin[0])  # warm (staging buffers)
-        barrier(pg)
-        t0 = time.perf_counter()
-        rc = lib.gb_execute_plan_1d_host_pipeline(hplan, outs_l, ins_l, e2e_steps)
-        el = time.perf_counter() - t0
-        if rc:
-            raise RuntimeError(lib.gb_last_error_string().decode())
-        el = max_over_ranks(pg, el)
+        # the host link is shared with the other GPUs' jobs on the machine:
+        # five timed runs of the steps, the median reported
+        runs = []
+        for _ in range(5):
+            barrier(pg)
+            t0 = time.perf_counter()
+            rc = lib.gb_execute_plan_1d_host_pipeline(hplan, outs_l, ins_l, e2e_steps)
+            el = time.perf_counter() - t0
+            if rc:
+                raise RuntimeError(lib.gb_last_error_string().decode())
+            runs.append(max_over_ranks(pg, el))
+        el = float(np.median(runs))
         last = (e2e_steps - 1) % 2
         piped = np.frombuffer((ctypes.c_char * nbytes).from_address(hout[last]), np.uint32).copy()
         t0 = time.perf_counter()
@@ -360,9 +365,10 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
         e2e = {"value": world * flops_step * e2e_steps / el / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "ms_per_step": 1e3 * el / e2e_steps, "steps": e2e_steps,
+               "runs_ms_per_step": [round(1e3 * r / e2e_steps, 4) for r in runs],
                "api": "mufft_gb_execute_plan_1d_host_pipeline over the steps' page-locked host buffers (each "
                       "step's input copied in and output copied out inside the timed region, copies of neighbouring "
-                      "steps overlapping)",
+                      "steps overlapping); median of five timed runs",
                "output_bitwise_equal_to_sync_api": e2e_ok,
                "sync_fft_h": {"value": world * flops_step * e2e_steps / el_sync / 1e9,
                               "ms_per_step": 1e3 * el_sync / e2e_steps,
