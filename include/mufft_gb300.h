@@ -126,6 +126,11 @@ typedef struct mufft_gb_options {
      * tiles wherever the tile has that variant (the 1024-thread 4096-point
      * column tile): -1 automatic (on), 0 off, 1 on */
     int persistent_tiles;
+    /* three-level transforms: the intermediate kept in L2 where it fits
+     * (stores marked evict-last, the input and output streamed evict-first,
+     * the intermediate dropped from L2 without write-back once the last pass
+     * has read it): -1 automatic, 0 off, 1 on */
+    int l2_residency;
 } mufft_gb_options;
 
 /* The defaults: levels 0, twiddles -1, fused 0, tma 0, occupancy 0, stream

@@ -156,7 +156,7 @@ class Options(C.Structure):
                 ("split_engine", C.c_int), ("columns_2d", C.c_int), ("conv_split", C.c_uint),
                 ("conv_classes", C.c_uint), ("stream_conv_ranges", C.c_uint), ("stream_conv_fused", C.c_int),
                 ("fft_split", C.c_uint), ("ntiles", C.c_uint), ("tiles", TileChoice * MAX_TILE_CHOICES),
-                ("persistent_tiles", C.c_int)]
+                ("persistent_tiles", C.c_int), ("l2_residency", C.c_int)]
 
 
 class MuFFTError(RuntimeError):

@@ -103,6 +103,13 @@ struct TileArgs {
     // transform index (column passes of a 2D four-step: W_N^(k*row) for every
     // column of the tile, from a per-CTA table)
     int tw_by_y;
+    // L2 residency of multi-pass intermediates (bits): L2_LOAD_FIRST plain
+    // loads marked evict-first, L2_STORE_LAST / L2_STORE_FIRST stores marked
+    // evict-last / evict-first, L2_DISCARD_IN the tile's input lines dropped
+    // from L2 without write-back once read (row tiles over a dead intermediate)
+    int l2;
 };
+
+constexpr int L2_LOAD_FIRST = 1, L2_STORE_LAST = 2, L2_STORE_FIRST = 4, L2_DISCARD_IN = 8;
 
 }  // namespace mgb

@@ -358,6 +358,31 @@ __device__ __forceinline__ float2 gload(const float2 *p)
         return __ldg(p);
 }
 
+// L2 cache policies (createpolicy) and the loads / stores that carry them.
+__device__ __forceinline__ unsigned long long l2_evict_first()
+{
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ unsigned long long l2_evict_last()
+{
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ float2 ld_policy(const float2 *p, unsigned long long pol)
+{
+    float2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st_policy(float2 *p, float2 v, unsigned long long pol)
+{
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
+                 : "memory");
+}
+
 template <int L, int R, int Q, int LMAP, bool COH = false>
 __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__restrict__ in,
                                             const float2 *__restrict__ in2, unsigned tr, int j, int tl,
@@ -378,6 +403,16 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
     const float2 *f = in + tbase + p0 * sst;
     switch (a.prologue) {
     case PRO_PLAIN: {
+        if (!COH && (a.l2 & L2_LOAD_FIRST)) {
+            const unsigned long long pol = l2_evict_first();
+#pragma unroll
+            for (int u = 0; u < NB; u++)
+#pragma unroll
+                for (int m = 0; m < r; m++)
+                    if (m < mlim)
+                        v[u * r + m] = ld_policy(f + (long long)(TL * u + m * Q * B) * sst, pol);
+            break;
+        }
 #pragma unroll
         for (int u = 0; u < NB; u++)
 #pragma unroll
@@ -821,6 +856,24 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         return;
     }
 
+    if constexpr (LMAP == ALONG && Q == 1 && NST > 1) {
+        // A dead intermediate: every thread has read its inputs (the stage
+        // exchanges' barriers lie between), so the tile's input lines leave L2
+        // without being written back.  Rows of L points at in_dist, 128-byte
+        // aligned (the planner sets the flag only then).
+        if (a.l2 & L2_DISCARD_IN) {
+            constexpr int LINES = L / 16;  // 128-byte lines per row
+            for (int idx = threadIdx.x; idx < C * LINES; idx += tile_threads<L, R, C, Q>()) {
+                const unsigned t = tile0 + idx / LINES;
+                if (t < a.ntrans) {
+                    const float2 *line = in + (long long)t * a.in_dist + 16 * (idx % LINES);
+                    asm volatile("discard.global.L2 [%0], 128;" ::"l"(line) : "memory");
+                }
+            }
+        }
+    }
+    const int l2st = a.l2 & (L2_STORE_LAST | L2_STORE_FIRST);
+    const unsigned long long stpol = (l2st & L2_STORE_LAST) ? l2_evict_last() : l2_evict_first();
     if (valid) {
         const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
         float2 *o0 = out + obase + (long long)p0 * sst;
@@ -851,7 +904,10 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     float2 y = cmul(v[u * rl + m], w);
                     if (a.conj & 2)
                         y.y = -y.y;
-                    o0[(long long)off * sst] = y;
+                    if (l2st)
+                        st_policy(&o0[(long long)off * sst], y, stpol);
+                    else
+                        o0[(long long)off * sst] = y;
                 }
         } else {
             const float sg = (a.conj & 2) ? -1.f : 1.f;
@@ -864,7 +920,10 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     if constexpr (EMUL)
                         y = cscale(cmul(y, __ldg(&a.in2[(long long)tr * a.in2_dist + (long long)(p0 + off) * a.in2_stride])),
                                    a.scale);
-                    o0[(long long)off * sst] = make_float2(y.x, sg * y.y);
+                    if (l2st)
+                        st_policy(&o0[(long long)off * sst], make_float2(y.x, sg * y.y), stpol);
+                    else
+                        o0[(long long)off * sst] = make_float2(y.x, sg * y.y);
                 }
         }
     }

@@ -74,7 +74,7 @@ const PersistTileKernel *find_persist(int L, int R, int C, int lmap, int smap);
 // (C, R, Q).
 struct PlanOptions {
     int levels = -2, twiddle = -2, fused = -2, tma = -2, occ = -2, stream = -2, split_engine = -2, cols2d = -2,
-        persist = -2;
+        persist = -2, l2 = -2;
     std::vector<TileKernel> tiles;
 };
 // The options of the plan being built on this thread (null: defaults).
@@ -101,6 +101,7 @@ int opt_stream();
 int opt_split_engine();
 int opt_cols2d();
 int opt_persist();
+int opt_l2();
 
 // ------------------------------------------------------------ device state
 

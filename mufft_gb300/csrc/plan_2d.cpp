@@ -245,9 +245,18 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
             pl->passes.push_back(c2);
         }
     } else if (kind == K2_C2R) {
+        if (opt_l2() == 1) {
+            // the column pass's output is the row pass's input only: kept in
+            // L2, dropped without write-back once read (rows of the scratch
+            // are whole 128-byte lines apart)
+            col.a.l2 = L2_LOAD_FIRST | L2_STORE_LAST;
+            row.a.l2 = L2_DISCARD_IN | L2_STORE_FIRST;
+        }
         pl->passes.push_back(col);
         pl->passes.push_back(row);
     } else {
+        if (opt_l2() == 1)  // the rows' output is what the column pass reads next
+            row.a.l2 = L2_LOAD_FIRST | L2_STORE_LAST;
         pl->passes.push_back(row);
         pl->passes.push_back(col);
     }

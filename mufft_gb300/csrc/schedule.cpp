@@ -652,6 +652,18 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
         pc.in_role = ROLE_SCRATCH;
         pc.out_role = s.out_role;
         pc.grid = dim3((N1 + kr->C - 1) / kr->C, N2 * s.batch);
+        if (opt_l2() == 1) {
+            // keep the intermediate in L2 as far as it fits: A streams its
+            // input and marks its stores evict-last, B (in place) keeps them
+            // so, C drops each row from L2 once read (its rows are 128-byte
+            // aligned: N3 >= 16 points at offsets of N3 points) and streams
+            // its output unless an r2c fix-up reads it next
+            pa.a.l2 = L2_LOAD_FIRST | L2_STORE_LAST;
+            pb.a.l2 = L2_STORE_LAST;
+            pc.a.l2 = (N3 >= 16 ? L2_DISCARD_IN : 0) | (r2c ? 0 : L2_STORE_FIRST);
+            out[out.size() - 2].a.l2 = pa.a.l2;
+            out[out.size() - 1].a.l2 = pb.a.l2;
+        }
         out.push_back(pc);
         if (r2c) {
             Pass p3;
@@ -735,6 +747,13 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p2.in_role = ROLE_SCRATCH;
     p2.out_role = s.out_role;
     p2.grid = dim3((N1 + kr->C - 1) / kr->C, s.batch);
+    if (opt_l2() == 1) {
+        // the intermediate as in the three-level schedule: kept in L2 by the
+        // first pass, dropped without write-back once the second has read it
+        // (rows of N2 >= 128 points, 128-byte aligned)
+        out.back().a.l2 = L2_LOAD_FIRST | L2_STORE_LAST;
+        p2.a.l2 = L2_DISCARD_IN | (r2c ? 0 : L2_STORE_FIRST);
+    }
     out.push_back(p2);
 
     if (r2c) {
