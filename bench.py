@@ -286,19 +286,24 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
     ms_max = max_over_ranks(pg, ms)
     ms_step = ms_max / args.steps
 
-    # per-kernel timing for the roofline (outside the headline region)
-    per_kernel = []
+    # per-kernel timing for the roofline (outside the headline region): each
+    # launch timed in place, inside whole steps (CUDA events between the
+    # launches of a step), so that it meets the cache state the launch before
+    # it leaves -- the passes hand their intermediate over in L2
+    per_kernel = [0.0] * launches
     reps = max(5, args.steps)
-    for k in range(launches):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        for i in range(reps):
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(launches + 1)] for _ in range(reps)]
+    for i in range(reps):
+        evs[i][0].record(st)
+        for k in range(launches):
             rc = lib.gb_execute_plan_1d_launches_async(plan, outs[i % nsets].data_ptr(), ins[i % nsets].data_ptr(),
                                                        k, 1, sp)
             assert rc == 0
-        e1.record(st)
-        torch.cuda.synchronize()
-        per_kernel.append(e0.elapsed_time(e1) / reps)
+            evs[i][k + 1].record(st)
+    torch.cuda.synchronize()
+    for i in range(reps):
+        for k in range(launches):
+            per_kernel[k] += evs[i][k].elapsed_time(evs[i][k + 1]) / reps
     # the same bytes moved by a device copy over the same rotating sets: the
     # memory system's ceiling for one pass of this size
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
