@@ -407,6 +407,13 @@ def run_ours(args, world, rank, local, pg) -> dict | None:
                      "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["source"] == "measured"
                      else "fallback 6.8 TB/s",
                      "per_kernel_ms": per_kernel,
+                     "per_kernel_timing": "each launch timed in place inside whole steps (CUDA events between "
+                                          "the launches), so a pass pays the write-backs the pass before it left",
+                     "step": {"algorithmic_bytes": algo_bytes_pass * launches,
+                              "achieved": algo_bytes_pass * launches / (ms_step * 1e-3) / 1e9,
+                              "frac": algo_bytes_pass * launches / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                              "frac_at_two_sweeps": 2 * 16 * elems / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"]
+                              if launches > 1 else None},
                      "frac_of_nominal_8tbs": achieved / 8000.0,
                      "same_bytes_device_copy_ms": copy_ms,
                      "frac_of_same_bytes_copy": copy_ms / per_kernel[dom]},
