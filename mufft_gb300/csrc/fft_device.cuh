@@ -873,7 +873,9 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         }
     }
     const int l2st = a.l2 & (L2_STORE_LAST | L2_STORE_FIRST);
-    const unsigned long long stpol = (l2st & L2_STORE_LAST) ? l2_evict_last() : l2_evict_first();
+    unsigned long long stpol = 0;
+    if (l2st)
+        stpol = (l2st & L2_STORE_LAST) ? l2_evict_last() : l2_evict_first();
     if (valid) {
         const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
         float2 *o0 = out + obase + (long long)p0 * sst;
