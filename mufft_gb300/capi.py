@@ -253,10 +253,21 @@ class MuFFT:
         return p
 
     # ---------------------------------------------------- numpy helpers
-    def fft_c2c(self, x: np.ndarray, direction: int, flags: int = 0, N: int | None = None) -> np.ndarray:
+    def _plan_1d(self, kind: int, N: int, direction: int, flags: int, opts):
+        """opts: mufft_gb_options for the GB300 library (None: the fft.h creator)."""
+        if opts is not None:
+            return self._plan(self.gb_create_plan_1d(kind, N, direction, flags, 1, 0, 0, C.byref(opts)),
+                              "gb_create_plan_1d")
+        if kind == 0:
+            return self._plan(self.create_plan_1d_c2c(N, direction, flags), "create_plan_1d_c2c")
+        if kind == 1:
+            return self._plan(self.create_plan_1d_r2c(N, flags), "create_plan_1d_r2c")
+        return self._plan(self.create_plan_1d_c2r(N, flags), "create_plan_1d_c2r")
+
+    def fft_c2c(self, x: np.ndarray, direction: int, flags: int = 0, N: int | None = None, opts=None) -> np.ndarray:
         x = aligned_copy(x, np.complex64)
         N = N or x.shape[-1]
-        plan = self._plan(self.create_plan_1d_c2c(N, direction, flags), "create_plan_1d_c2c")
+        plan = self._plan_1d(0, N, direction, flags, opts)
         out = aligned_zeros(N, np.complex64)
         try:
             self.execute_plan_1d(plan, _ptr(out), _ptr(x))
@@ -265,10 +276,10 @@ class MuFFT:
             self.free_plan_1d(plan)
         return out
 
-    def fft_r2c(self, x: np.ndarray, flags: int = 0, N: int | None = None) -> np.ndarray:
+    def fft_r2c(self, x: np.ndarray, flags: int = 0, N: int | None = None, opts=None) -> np.ndarray:
         x = aligned_copy(x, np.float32)
         N = N or x.shape[-1]
-        plan = self._plan(self.create_plan_1d_r2c(N, flags), "create_plan_1d_r2c")
+        plan = self._plan_1d(1, N, FORWARD, flags, opts)
         nout = N if flags & FLAG_FULL_R2C else N // 2 + 1
         out = aligned_zeros(nout, np.complex64)
         try:
@@ -278,10 +289,10 @@ class MuFFT:
             self.free_plan_1d(plan)
         return out
 
-    def fft_c2r(self, X: np.ndarray, N: int, flags: int = 0) -> np.ndarray:
+    def fft_c2r(self, X: np.ndarray, N: int, flags: int = 0, opts=None) -> np.ndarray:
         X = aligned_copy(X, np.complex64)
         assert X.shape[-1] >= N // 2 + 1
-        plan = self._plan(self.create_plan_1d_c2r(N, flags), "create_plan_1d_c2r")
+        plan = self._plan_1d(2, N, INVERSE, flags, opts)
         out = aligned_zeros(N, np.float32)
         try:
             self.execute_plan_1d(plan, _ptr(out), _ptr(X))

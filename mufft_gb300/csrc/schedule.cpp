@@ -234,6 +234,14 @@ std::string describe(const std::vector<Pass> &ps)
         else
             snprintf(buf, sizeof(buf), "%sr2c_fixup M=%lld batch=%u full=%d", i ? "; " : "", p.M, p.batch, p.full);
         s += buf;
+        if (p.type == PASS_TILE && p.a.l2) {
+            // L2 policy: loads evict-first, stores evict-last / evict-first, input discarded
+            s += " l2=";
+            s += (p.a.l2 & L2_LOAD_FIRST) ? "F" : "";
+            s += (p.a.l2 & L2_STORE_LAST) ? "L" : "";
+            s += (p.a.l2 & L2_STORE_FIRST) ? "S" : "";
+            s += (p.a.l2 & L2_DISCARD_IN) ? "D" : "";
+        }
     }
     return s;
 }

@@ -250,6 +250,24 @@ def test_schedule_options_in_dry_runs(lib):
     s = _sched(lib, 1 << 24, 0, opts=lib.options(multipass_levels=2, persistent_tiles=0))
     assert "+persistent" not in s and "grid=1024x1" in s, s
     assert "+persistent" not in _sched(lib, 1 << 24, 0)
+
+
+def test_l2_residency_hints_in_schedules(lib):
+    """Multi-pass intermediates carry L2 cache-policy hints by default: the
+    first pass streams its input and keeps its output (F, L), the last drops
+    the intermediate once read and streams its output (D, S; no S before an
+    r2c fix-up, which reads that output); single passes carry none."""
+    a, b, c = _sched(lib, 1 << 24, 0).split("; ")
+    assert a.endswith("l2=FL") and b.endswith("l2=L") and c.endswith("l2=SD"), (a, b, c)
+    p1, p2, fix = _sched(lib, 1 << 21, 1).split("; ")
+    assert p1.endswith("l2=FL") and p2.endswith("l2=D") and fix.startswith("r2c_fixup"), (p1, p2)
+    assert "l2=" not in _sched(lib, 1 << 24, 0, opts=lib.options(l2_residency=0))
+    assert "l2=" not in _sched(lib, 4096, 0, batch=64)
+    buf = C.create_string_buffer(64)
+    for v in (2, -2):
+        o = lib.options(l2_residency=v)
+        assert lib.gb_describe_schedule_1d(1024, 0, K.FORWARD, 0, 1, C.byref(o), buf, 64) == -1
+        lib.gb_clear_error()
     buf = C.create_string_buffer(64)
     for bad in (dict(tile_occupancy=-1), dict(tile_occupancy=33), dict(stream_tiles=2), dict(stream_conv_fused=3),
                 dict(stream_conv_ranges=1 << 21), dict(conv_split=1000), dict(twiddle_table=3), dict(tma=3),
@@ -266,7 +284,7 @@ def test_schedule_options_in_dry_runs(lib):
     lib.gb_clear_error()
     d = lib.options()
     assert (d.multipass_levels, d.twiddle_table, d.conv_split, d.conv_classes, d.stream_conv_fused,
-            d.persistent_tiles) == (0, -1, 65536, 16384, 1, -1)
+            d.persistent_tiles, d.l2_residency) == (0, -1, 65536, 16384, 1, -1, -1)
 
 
 def test_batched_convolution_entry_points_validate_on_host(lib):

@@ -233,6 +233,33 @@ def test_2d_persistent_columns_match_oracle(gpu, ora, Nx):
         assert_close(a, ora.fft2_c2c(X, d), Nx * Ny, what=f"2d c2c {Nx}x{Ny} {d}")
 
 
+def test_l2_residency_hints_change_no_bits(gpu, ora):
+    """The L2 cache-policy hints (and the discard of dead intermediates) leave
+    every output bit unchanged: three-level c2c 2^22, four-step r2c / c2r
+    batches, 2D c2r with a discarded scratch; the hinted results also against
+    the oracle / FP64."""
+    on, off = gpu.options(l2_residency=1), gpu.options(l2_residency=0)
+    same = lambda u, v: np.array_equal(u.view(np.uint32), v.view(np.uint32))  # noqa: E731
+    N = 1 << 22
+    x = signals.complex_uniform(14000, N)
+    a, b = gpu.fft_c2c(x, K.FORWARD, opts=on), gpu.fft_c2c(x, K.FORWARD, opts=off)
+    assert same(a, b)
+    assert rel_l2(a, np.fft.fft(x.astype(np.complex128))) < 2e-6
+    N = 1 << 21
+    r = signals.uniform(14050, N)
+    a, b = gpu.fft_r2c(r, opts=on), gpu.fft_r2c(r, opts=off)
+    assert same(a, b)
+    assert rel_l2(a, np.fft.rfft(r.astype(np.float64))) < 2e-6
+    back, back0 = gpu.fft_c2r(a, N, opts=on), gpu.fft_c2r(a, N, opts=off)
+    assert same(back, back0)
+    assert rel_l2(back / N, r) < 4e-6
+    Nx, Ny = 256, 4096
+    X = signals.complex_uniform(14100, Nx * Ny).reshape(Ny, Nx)
+    c, d = gpu.fft2_c2r(X, opts=on), gpu.fft2_c2r(X, opts=off)
+    assert np.array_equal(c.view(np.uint32), d.view(np.uint32))
+    assert_close(c, ora.fft2_c2r(X), Nx * Ny, what="2d c2r 256x4096")
+
+
 def test_2d_4096_round_trip(gpu):
     Nx = Ny = 4096
     x = signals.normal(13000, Nx * Ny).reshape(Ny, Nx)
