@@ -688,6 +688,7 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     }
 
     // Four-step: M = N1 * N2, x[n1*N2 + n2], X[k1 + N1*k2].
+    constexpr size_t kL2HintMaxScratch = (size_t)128 << 20;  // about the L2 of a GB300
     const unsigned N1 = 1u << (lg / 2), N2 = M / N1;
     if (N2 > kMaxTile) {
         set_error(MUFFT_GB_ERR_UNSUPPORTED, "transform length %u exceeds the two-pass limit", M);
@@ -755,10 +756,13 @@ bool build_fft_passes(const FftSpec &s, const float2 *tw, PlanResources &res, bo
     p2.in_role = ROLE_SCRATCH;
     p2.out_role = s.out_role;
     p2.grid = dim3((N1 + kr->C - 1) / kr->C, s.batch);
-    if (opt_l2() == 1) {
+    if (opt_l2() == 1 && (size_t)M * s.batch * sizeof(float2) <= kL2HintMaxScratch) {
         // the intermediate as in the three-level schedule: kept in L2 by the
         // first pass, dropped without write-back once the second has read it
-        // (rows of N2 >= 128 points, 128-byte aligned)
+        // (rows of N2 >= 128 points, 128-byte aligned).  Only where it about
+        // fits: for larger batches the hints measured slower (c2c 2^21 x 64
+        // 917 -> 957 us, 2^20 x 128 857 -> 898 us, 2^21 x 16 246 -> 253 us)
+        // against 2^16 x 256 94.2 -> 89.6 us and r2c 2^21 x 8 101.6 -> 94.0 us.
         out.back().a.l2 = L2_LOAD_FIRST | L2_STORE_LAST;
         p2.a.l2 = L2_DISCARD_IN | (r2c ? 0 : L2_STORE_FIRST);
     }
