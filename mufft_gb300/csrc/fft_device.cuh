@@ -371,6 +371,12 @@ __device__ __forceinline__ unsigned long long l2_evict_last()
     asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+__device__ __forceinline__ unsigned long long l2_evict_normal()
+{
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
 __device__ __forceinline__ float2 ld_policy(const float2 *p, unsigned long long pol)
 {
     float2 v;
@@ -403,22 +409,22 @@ __device__ __forceinline__ void load_stage0(const TileArgs &a, const float2 *__r
     const float2 *f = in + tbase + p0 * sst;
     switch (a.prologue) {
     case PRO_PLAIN: {
-        if (!COH && (a.l2 & L2_LOAD_FIRST)) {
-            const unsigned long long pol = l2_evict_first();
-#pragma unroll
-            for (int u = 0; u < NB; u++)
-#pragma unroll
-                for (int m = 0; m < r; m++)
-                    if (m < mlim)
-                        v[u * r + m] = ld_policy(f + (long long)(TL * u + m * Q * B) * sst, pol);
-            break;
-        }
+        // read-only loads carry an L2 policy: evict-first for a pass that
+        // streams its input, else evict-normal
+        unsigned long long pol = 0;
+        if constexpr (!COH)
+            pol = (a.l2 & L2_LOAD_FIRST) ? l2_evict_first() : l2_evict_normal();
 #pragma unroll
         for (int u = 0; u < NB; u++)
 #pragma unroll
             for (int m = 0; m < r; m++)
-                if (m < mlim)
-                    v[u * r + m] = gload<COH>(f + (long long)(TL * u + m * Q * B) * sst);
+                if (m < mlim) {
+                    const float2 *src = f + (long long)(TL * u + m * Q * B) * sst;
+                    if constexpr (COH)
+                        v[u * r + m] = gload<COH>(src);
+                    else
+                        v[u * r + m] = ld_policy(src, pol);
+                }
         break;
     }
     case PRO_MUL: {
@@ -873,9 +879,12 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
         }
     }
     const int l2st = a.l2 & (L2_STORE_LAST | L2_STORE_FIRST);
-    unsigned long long stpol = 0;
-    if (l2st)
-        stpol = (l2st & L2_STORE_LAST) ? l2_evict_last() : l2_evict_first();
+    // every store carries an L2 policy (evict-normal unless the pass asks
+    // for another): one instruction form whatever the pass, no branch per
+    // store (measured: 2^24 136.2 -> 130-131 us, 4096^2 c2c 131.4 -> 125.8 us
+    // against plain stores beside hinted ones)
+    const unsigned long long stpol =
+        (l2st & L2_STORE_LAST) ? l2_evict_last() : (l2st ? l2_evict_first() : l2_evict_normal());
     if (valid) {
         const long long sst = (SMAP == ALONG) ? 1 : a.out_stride;
         float2 *o0 = out + obase + (long long)p0 * sst;
@@ -906,10 +915,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     float2 y = cmul(v[u * rl + m], w);
                     if (a.conj & 2)
                         y.y = -y.y;
-                    if (l2st)
-                        st_policy(&o0[(long long)off * sst], y, stpol);
-                    else
-                        o0[(long long)off * sst] = y;
+                    st_policy(&o0[(long long)off * sst], y, stpol);
                 }
         } else {
             const float sg = (a.conj & 2) ? -1.f : 1.f;
@@ -922,10 +928,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
                     if constexpr (EMUL)
                         y = cscale(cmul(y, __ldg(&a.in2[(long long)tr * a.in2_dist + (long long)(p0 + off) * a.in2_stride])),
                                    a.scale);
-                    if (l2st)
-                        st_policy(&o0[(long long)off * sst], make_float2(y.x, sg * y.y), stpol);
-                    else
-                        o0[(long long)off * sst] = make_float2(y.x, sg * y.y);
+                    st_policy(&o0[(long long)off * sst], make_float2(y.x, sg * y.y), stpol);
                 }
         }
     }
