@@ -1,7 +1,7 @@
 #!/bin/sh
 # Compiles the reference muFFT library from its own sources into
-# oracle/_ref/libmufft_ref.so (a checker only: golden-vector generation and
-# CPU-side parity of the oracle restatement).  The reference's CMake build is
+# oracle/_ref/libmufft_ref.so (test infrastructure only: golden-vector
+# generation and CPU-side parity of the oracle restatement).  The reference's CMake build is
 # not used; this is the same set of translation units and per-file ISA flags
 # (CMakeLists.txt:23-63) driven by gcc directly.  Nothing is copied: the
 # sources are read where they lie.

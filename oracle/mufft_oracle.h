@@ -1,8 +1,8 @@
 /*
  * mufft_oracle.h -- CPU restatement of muFFT's scalar FFT / convolution path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the parity checker for the CUDA library in
- * mufft_gb300/.  Only tests/, __graft_entry__.smoke() and the CPU-baseline leg
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA library in
+ * mufft_gb300/ is compared against.  Only tests/, __graft_entry__.smoke() and the CPU-baseline leg
  * of bench.py load it; the shipped library never links or calls it.
  *
  * The functions mirror the reference public API (fft.h) one for one, with an
