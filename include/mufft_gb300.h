@@ -136,7 +136,7 @@ typedef struct mufft_gb_options {
 /* The defaults: levels 0, twiddles -1, fused 0, tma 0, occupancy 0, stream
  * tiles 0, split engine 0, 2D columns 0, conv_split 65536, conv_classes
  * 16384, stream ranges 0, stream fused 1, fft_split 8192, no tile choices,
- * persistent tiles -1. */
+ * persistent tiles -1, L2 residency -1. */
 void mufft_gb_options_init(mufft_gb_options *opts);
 
 /* 1D plans of every kind with options: kind 0 c2c, 1 r2c, 2 c2r (direction
