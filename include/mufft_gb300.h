@@ -104,7 +104,8 @@ typedef struct mufft_gb_options {
     /* split-precision products on tcgen05.mma with TMEM (0) or mma.sync (1) */
     int split_engine;
     /* 2D columns: 0 automatic (8192 points and more as a two-pass four-step
-     * of short, wide column tiles), 1 one pass, 2 two passes where possible */
+     * of short, wide column tiles, and 4096 points for grids at least 4096
+     * (real) or 8192 (c2c) wide), 1 one pass, 2 two passes where possible */
     int columns_2d;
     /* ragged convolution batches: requests of at least conv_split complex
      * points run as phase tasks over many CTAs (0: none), of at least

@@ -878,6 +878,22 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, unsigned tile, int 
             }
         }
     }
+    if constexpr (LMAP == ACROSS && Q == 1 && NST > 1 && C * 8 >= 128) {
+        // The same for a column tile over a dead intermediate: its input is L
+        // row segments of C neighbouring columns (in_dist 1), C * 8 / 128
+        // lines each, 128-byte aligned (the planner sets the flag only then);
+        // lines that start past the last column are not the tile's.
+        if (a.l2 & L2_DISCARD_IN) {
+            constexpr int LPR = C * 8 / 128;
+            for (int idx = threadIdx.x; idx < L * LPR; idx += tile_threads<L, R, C, Q>()) {
+                const unsigned col = tile0 + 16 * (idx % LPR);
+                if (col < a.ntrans) {
+                    const float2 *line = in + col + (long long)(idx / LPR) * a.in_stride;
+                    asm volatile("discard.global.L2 [%0], 128;" ::"l"(line) : "memory");
+                }
+            }
+        }
+    }
     const int l2st = a.l2 & (L2_STORE_LAST | L2_STORE_FIRST);
     // every store carries an L2 policy (evict-normal unless the pass asks
     // for another): one instruction form whatever the pass, no branch per

@@ -151,7 +151,8 @@ thread_local const PlanOptions *t_opts = nullptr;
 //    per-thread loads at four CTAs per SM (the autotuner still tries them);
 //  - no resident-CTA cap, no streaming row tiles (both measured slower);
 //  - split-precision products on tcgen05.mma;
-//  - 2D columns: two-pass four-step from 8192 points;
+//  - 2D columns: two-pass four-step from 8192 points, and from 4096 for
+//    wide grids (Nx >= 4096 real, >= 8192 c2c) when the L2 hints are on;
 //  - persistent tile grids wherever the tile has that variant (the
 //    1024-thread 4096-point column tile);
 //  - multi-pass intermediates kept in L2 by cache-policy hints and dropped

@@ -176,15 +176,21 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
     // passes of short column tiles (C1: length N1 at stride N2 rows, twiddle
     // W_Ny^(k1*n2) with n2 the grid row; C2: length N2, stored transposed to
     // rows k1 + N1*k2) -- 64-column tiles instead of the 1-2-column tiles a
-    // whole 8192- or 16384-point column allows.  At Ny = 4096 the one-pass
-    // 4-column tiles measured as fast or faster (4096^2 r2c columns 41.3 us
-    // vs 18.6 + 26.8 us; c2c 84.8 vs 53.4 + 43.2 us), so the automatic choice
-    // starts at 8192.
+    // whole 8192- or 16384-point column allows.  With the intermediate kept in
+    // L2 (cache-policy hints) the two passes also win at Ny = 4096 for wide
+    // grids; measured (us, r2c / c2r / c2c, one pass -> two passes): 4096 x
+    // 4096 72.0 / 82.7 / 125.9 -> 69.1 / 79.5 / 130.1, 8192 x 4096 160.1 /
+    // 160.4 / 313.7 -> 141.5 / 159.5 / 289.0, 16384 x 4096 356.2 / 397.2 /
+    // 708.9 -> 306.9 / 358.9 / 633.3, but 2048 x 4096 39.1 / 43.9 / 65.8 ->
+    // 41.1 / 44.7 / 63.0 and 4096 x 2048 or 16384 x 2048 slower in every
+    // kind.  So the automatic choice: Ny >= 8192, or Ny = 4096 with Nx >= 4096
+    // (real) / Nx >= 8192 (c2c); without the hints one pass up to 4096.
     const int mode = opt_cols2d();
     const unsigned lgy = ilog2u(Ny);
     const unsigned N1 = 1u << (lgy / 2), N2 = Ny / N1;
     const TileKernel *kc1 = find_tile((int)N1, ACROSS, ACROSS), *kc2 = find_tile((int)N2, ACROSS, ACROSS);
-    if ((mode == 2 || (mode == 0 && Ny >= 8192)) && N1 >= 2 && kc1 && kc2) {
+    const bool wide = opt_l2() == 1 && Ny >= 4096 && Nx >= (kind == K2_C2C ? 8192u : 4096u);
+    if ((mode == 2 || (mode == 0 && (Ny >= 8192 || wide))) && N1 >= 2 && kc1 && kc2) {
         const unsigned ncols = (unsigned)col.a.ntrans;
         const long long s_in = col.a.in_stride;                                 // pitch the columns are read at
         const long long s_out = kind == K2_C2R ? col.a.out_stride : (long long)Nx;  // pitch of C1 / C2 outputs
@@ -233,6 +239,19 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         c2.in_role = ROLE_SCRATCH;
         c2.out_role = c2_out;
         c2.grid = dim3((ncols + kc2->C - 1) / kc2->C, N1);
+        if (opt_l2() == 1) {
+            // intermediates kept in L2 and dropped once read, as in the
+            // one-pass forms: C2 reads whole 128-byte lines of C1's output
+            // (64-column tiles at a pitch of whole lines) when its tile is at
+            // least 16 columns wide
+            const bool lines = kc2->C >= 16 && (s_out % 16) == 0;
+            c1.a.l2 = kind == K2_C2R ? (L2_LOAD_FIRST | L2_STORE_LAST) : L2_STORE_LAST;
+            c2.a.l2 = (lines ? L2_DISCARD_IN : 0) | (kind == K2_C2R ? L2_STORE_LAST : L2_STORE_FIRST);
+            if (kind == K2_C2R)
+                row.a.l2 = L2_DISCARD_IN | L2_STORE_FIRST;
+            else
+                row.a.l2 = L2_LOAD_FIRST | L2_STORE_LAST;
+        }
         if (kind == K2_C2R) {
             row.in_role = ROLE_SCRATCH2;
             pl->passes.push_back(c1);
