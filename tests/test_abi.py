@@ -252,6 +252,16 @@ def test_schedule_options_in_dry_runs(lib):
     assert "+persistent" not in _sched(lib, 1 << 24, 0)
 
 
+def test_options_struct_layout_matches_the_header(lib):
+    """mufft_gb_options_init writes sizeof(mufft_gb_options) into `size`:
+    the ctypes mirror has the same size, and the fields after the tile choices
+    (appended later) land where the library reads them."""
+    o = K.Options()
+    lib.gb_options_init(C.byref(o))
+    assert o.size == C.sizeof(K.Options)
+    assert (o.persistent_tiles, o.l2_residency, o.fft_split, o.ntiles) == (-1, -1, 8192, 0)
+
+
 def test_l2_residency_hints_in_schedules(lib):
     """Multi-pass intermediates carry L2 cache-policy hints by default: the
     first pass streams its input and keeps its output (F, L), the last drops
