@@ -395,9 +395,14 @@ bool attach_persist(std::vector<Pass> &ps, bool dry, int device)
             continue;
         int sms = 152, per_sm = 1;
         if (!dry) {
+            // the kernel's limit is the device's opt-in maximum, so that no
+            // plan created later lowers it under an earlier plan's launch
+            // (with or without the twiddle region, any resident-CTA cap)
             const size_t smem = tile_launch_smem(p);
+            int limit = 232448;
+            cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-            if (!cuda_ok(cudaFuncSetAttribute(pt->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            if (!cuda_ok(cudaFuncSetAttribute(pt->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, limit),
                          "cudaFuncSetAttribute(persist)") ||
                 !cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt->fn, pt->threads, smem),
                          "occupancy(persist)"))

@@ -13,6 +13,7 @@ import pytest
 
 from helpers import REL_L2_TOL, direct_conv_f64, golden, golden_cases, max_abs, rel_l2
 from mufft_gb300 import capi as K
+from mufft_gb300.capi import aligned_copy
 from mufft_gb300 import signals
 
 pytestmark = pytest.mark.gpu
@@ -231,6 +232,26 @@ def test_2d_persistent_columns_match_oracle(gpu, ora, Nx):
         a, b = gpu.fft2_c2c(X, d, opts=on), gpu.fft2_c2c(X, d, opts=off)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
         assert_close(a, ora.fft2_c2c(X, d), Nx * Ny, what=f"2d c2c {Nx}x{Ny} {d}")
+
+
+def test_persistent_column_plans_created_in_any_order(gpu):
+    """The persistent 4096-point column tile serves launches with the twiddle
+    region (1D four-step 4096 x 4096) and without it (2D columns): a plan
+    created afterwards must not lower the kernel's shared-memory limit under
+    the earlier plan's launch."""
+    N = 1 << 24
+    four_step = gpu._plan_1d(0, N, K.FORWARD, 0, gpu.options(multipass_levels=2))
+    try:
+        xr = signals.uniform(14200, 2048 * 4096).reshape(4096, 2048)
+        X = gpu.fft2_r2c(xr)  # one-pass persistent columns, no twiddle region
+        assert rel_l2(X[:, :1025], np.fft.rfft2(xr.astype(np.float64))) < 2e-6
+        x = aligned_copy(signals.complex_uniform(14300, N), np.complex64)
+        y = np.zeros(N, np.complex64)
+        gpu.execute_plan_1d(four_step, y.ctypes.data, x.ctypes.data)
+        gpu.check("execute_plan_1d")
+        assert rel_l2(y, np.fft.fft(x.astype(np.complex128))) < 2e-6
+    finally:
+        gpu.free_plan_1d(four_step)
 
 
 def test_l2_residency_hints_change_no_bits(gpu, ora):
