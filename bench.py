@@ -7,12 +7,16 @@ roofline" is quoted on), through libmufft_gb300's C ABI:
 
   value     GFLOP/s = 5 N log2 N / device time per step, inputs resident in HBM,
             rotating over 4 input/output buffer sets of 256 MiB (larger than L2)
-  e2e       the same metric through mufft_execute_plan_1d() on pinned host
-            buffers: host->device copy, both kernels, device->host copy per step
+  e2e       the same metric through the C ABI on page-locked host buffers,
+            every step's host->device copy and device->host copy inside the
+            timed region: mufft_gb_execute_plan_1d_host_pipeline (copies of
+            neighbouring steps overlap the kernels; median of five runs), with
+            mufft_execute_plan_1d() per step beside it
   roofline  the dominant kernel's algorithmic bytes per launch / its average
-            CUDA-event duration, against the measured HBM copy bandwidth; also
-            a device copy of the same bytes over the same rotating buffers
-            (the memory system's ceiling for one pass of this size)
+            CUDA-event duration, each launch timed in place inside whole steps,
+            against the measured HBM copy bandwidth; the whole step's figure
+            beside it; also a device copy of the same bytes over the same
+            rotating buffers (the memory system's ceiling for one pass)
   cpu_baseline  the reference's scalar C path (the oracle port, or the
             reference itself where it was compiled) on all host cores, one
             independent 2^24 transform per thread
