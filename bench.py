@@ -53,7 +53,7 @@ METRIC = "c2c GFLOP/s (5N·log2N) + % HBM roofline; split-TC vs FP32 at equal FP
 
 # name -> (N, batch, description)
 WORKLOADS = {
-    "c2c_2^24": (1 << 24, 1, "c2c forward, N=2^24 complex64, one transform per step (four-step 4096 x 4096)"),
+    "c2c_2^24": (1 << 24, 1, "c2c forward, N=2^24 complex64, one transform per step (multi-pass)"),
     "c2c_4096x65536": (4096, 65536, "c2c forward, batch 65536 x N=4096 complex64 (single pass)"),
     "c2c_1024x4096": (1024, 4096, "c2c forward, batch 4096 x N=1024 complex64 (single pass)"),
 }
