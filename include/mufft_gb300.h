@@ -424,6 +424,11 @@ int mufft_gb_plan_2d_describe(const mufft_plan_2d *plan, char *buf, size_t size)
 int mufft_gb_describe_schedule_1d(unsigned N, int kind, int direction, unsigned flags, unsigned batch,
                                   const mufft_gb_options *opts, char *buf, size_t size);
 
+/* The same for a 2D plan (kind 0 c2c, 1 r2c, 2 c2r; Nx columns, Ny rows;
+ * direction is used by c2c only), without touching a GPU. */
+int mufft_gb_describe_schedule_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsigned flags,
+                                  const mufft_gb_options *opts, char *buf, size_t size);
+
 /* --------------------------------------------------------- autotuning */
 
 /* Times the candidate GPU schedules of a 1D plan shape (kind 0 c2c, 1 r2c,

@@ -84,6 +84,7 @@ GB_H = [
     ("plan_1d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("plan_2d_describe", _i, [_vp, C.c_char_p, _sz]),
     ("describe_schedule_1d", _i, [_u, _i, _i, _u, _u, _vp, C.c_char_p, _sz]),
+    ("describe_schedule_2d", _i, [_i, _u, _u, _i, _u, _vp, C.c_char_p, _sz]),
     ("options_init", None, [_vp]),
     ("create_plan_1d", _vp, [_i, _u, _i, _u, _u, _sz, _sz, _vp]),
     ("create_plan_2d", _vp, [_i, _u, _u, _i, _u, _vp]),

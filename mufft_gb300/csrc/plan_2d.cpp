@@ -41,7 +41,9 @@ void destroy_2d(mufft_plan_2d *pl)
     delete pl;
 }
 
-mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsigned flags)
+// dry: the schedule only (into `desc`), without touching a GPU; returns null.
+mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsigned flags, bool dry = false,
+                         std::string *desc = nullptr)
 {
     t_err = 0;
     if (!is_pow2(Nx) || !is_pow2(Ny) || Nx == 1 || Ny == 1) {
@@ -67,8 +69,8 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         set_error(MUFFT_GB_ERR_UNSUPPORTED, "no 2D kernels for %u x %u", Nx, Ny);
         return nullptr;
     }
-    int dev;
-    if (!device_prepare(&dev))
+    int dev = 0;
+    if (!dry && !device_prepare(&dev))
         return nullptr;
     mufft_plan_2d *pl = new mufft_plan_2d();
     pl->device = dev;
@@ -78,14 +80,14 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
     pl->Mx = Mx;
     pl->flags = flags;
     pl->direction = kind == K2_C2C ? direction : (kind == K2_R2C ? MUFFT_FORWARD : MUFFT_INVERSE);
-    const float2 *tw = g_dev[dev].tw;
+    const float2 *tw = dry ? nullptr : g_dev[dev].tw;
     const bool inv = pl->direction == MUFFT_INVERSE;
     const bool full = (flags & MUFFT_FLAG_FULL_R2C) != 0;
-    if (!cuda_ok(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
+    if (!dry && !cuda_ok(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
         destroy_2d(pl);
         return nullptr;
     }
-    if (kind != K2_C2C) {
+    if (kind != K2_C2C && !dry) {
         pl->res.rtw = upload(r2c_twiddles(kind == K2_R2C ? MUFFT_FORWARD : MUFFT_INVERSE, Mx));
         if (!pl->res.rtw) {
             destroy_2d(pl);
@@ -148,7 +150,7 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         // column tiles then store full sectors
         const size_t sstride = ((size_t)Mx + 1 + 15) & ~(size_t)15;
         pl->res.scratch_bytes = sstride * Ny * sizeof(float2);
-        if (!cuda_ok(cudaMalloc(&pl->res.scratch, pl->res.scratch_bytes), "cudaMalloc(scratch)")) {
+        if (!dry && !cuda_ok(cudaMalloc(&pl->res.scratch, pl->res.scratch_bytes), "cudaMalloc(scratch)")) {
             destroy_2d(pl);
             return nullptr;
         }
@@ -198,12 +200,12 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         const Role c1_out = ROLE_SCRATCH;
         const Role c2_out = kind == K2_C2R ? ROLE_SCRATCH2 : ROLE_OUT;
         const size_t bytes = (size_t)Ny * (size_t)s_out * sizeof(float2);
-        if (kind != K2_C2R) {
+        if (kind != K2_C2R && !dry) {
             cudaFree(pl->res.scratch);
             pl->res.scratch = nullptr;
         }
-        if ((!pl->res.scratch && !cuda_ok(cudaMalloc(&pl->res.scratch, bytes), "cudaMalloc(scratch)")) ||
-            (kind == K2_C2R && !cuda_ok(cudaMalloc(&pl->res.scratch2, bytes), "cudaMalloc(scratch)"))) {
+        if (!dry && ((!pl->res.scratch && !cuda_ok(cudaMalloc(&pl->res.scratch, bytes), "cudaMalloc(scratch)")) ||
+                     (kind == K2_C2R && !cuda_ok(cudaMalloc(&pl->res.scratch2, bytes), "cudaMalloc(scratch)")))) {
             destroy_2d(pl);
             return nullptr;
         }
@@ -279,9 +281,18 @@ mufft_plan_2d *create_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsi
         pl->passes.push_back(row);
         pl->passes.push_back(col);
     }
-    if (!attach_stream(pl->passes, false, pl->device) || !attach_persist(pl->passes, false, pl->device) ||
-        !attach_occupancy(pl->passes, false, pl->device)) {
-        destroy_2d(pl);
+    if (!attach_stream(pl->passes, dry, pl->device) || !attach_persist(pl->passes, dry, pl->device) ||
+        !attach_occupancy(pl->passes, dry, pl->device)) {
+        if (dry)
+            delete pl;
+        else
+            destroy_2d(pl);
+        return nullptr;
+    }
+    if (desc)
+        *desc = describe(pl->passes);
+    if (dry) {
+        delete pl;  // nothing was allocated
         return nullptr;
     }
     return pl;
@@ -363,6 +374,28 @@ mufft_plan_2d *mufft_gb_create_plan_2d(int kind, unsigned Nx, unsigned Ny, int d
     OptionsScope scope(opts ? &o : nullptr);
     return create_2d(kind, Nx, Ny, kind == K2_C2C ? direction : (kind == K2_R2C ? MUFFT_FORWARD : MUFFT_INVERSE),
                      flags);
+}
+
+int mufft_gb_describe_schedule_2d(int kind, unsigned Nx, unsigned Ny, int direction, unsigned flags,
+                                  const mufft_gb_options *opts, char *buf, size_t size)
+{
+    t_err = 0;
+    if (kind < K2_C2C || kind > K2_C2R) {
+        set_error(MUFFT_GB_ERR_INVALID, "kind must be 0 (c2c), 1 (r2c) or 2 (c2r)");
+        return MUFFT_GB_ERR_INVALID;
+    }
+    PlanOptions o;
+    if (opts && !convert_options(opts, &o))
+        return t_err;
+    OptionsScope scope(opts ? &o : nullptr);
+    std::string d;
+    create_2d(kind, Nx, Ny, kind == K2_C2C ? direction : (kind == K2_R2C ? MUFFT_FORWARD : MUFFT_INVERSE), flags,
+              true, &d);
+    if (t_err)
+        return t_err;
+    if (buf && size)
+        snprintf(buf, size, "%s", d.c_str());
+    return MUFFT_GB_OK;
 }
 
 void mufft_execute_plan_2d(mufft_plan_2d *plan, void *MUFFT_RESTRICT output, const void *MUFFT_RESTRICT input)

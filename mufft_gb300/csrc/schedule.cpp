@@ -221,7 +221,8 @@ std::string describe(const std::vector<Pass> &ps)
                      i ? "; " : "", p.tk ? (p.tk->nbuf == 2 ? "+tma2" : "+tma1") : (p.sk ? "+stream" : (p.pt ? "+persistent" : "")), p.k->L, p.k->R, p.k->C, p.k->Q, p.k->lmap ? "across" : "along",
                      p.k->smap ? "across" : "along", p.sk ? p.sk_grid : (p.pt ? std::min(p.grid.x * p.grid.y, p.pt_grid) : p.grid.x), p.pt ? 1u : p.grid.y, p.k->threads, std::max(p.k->smem, p.smem_min),
                      pro_name(p.a.prologue), p.a.half ? "+half" : "", epi_name(p.a.epilogue),
-                     p.a.epilogue != EPI_TWIDDLE ? "" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos")),
+                     p.a.epilogue != EPI_TWIDDLE ? ""
+                     : (p.a.tw_by_y ? "/by_row" : (p.a.tw_colpow ? "/colpow" : (p.a.tw_lo ? "/table" : "/sincos"))),
                      p.a.conj);
         else if (p.type == PASS_SPLIT)
             snprintf(buf, sizeof(buf), "%ssplit_tc N=%d bf16x%d %s grid=%u threads=%d smem=%zu conj=%d", i ? "; " : "",

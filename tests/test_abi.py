@@ -262,6 +262,38 @@ def test_options_struct_layout_matches_the_header(lib):
     assert (o.persistent_tiles, o.l2_residency, o.fft_split, o.ntiles) == (-1, -1, 8192, 0)
 
 
+def _sched2d(lib, kind, Nx, Ny, opts=None):
+    buf = C.create_string_buffer(4096)
+    rc = lib.gb_describe_schedule_2d(kind, Nx, Ny, K.FORWARD, 0, C.byref(opts) if opts else None, buf, 4096)
+    assert rc == 0, (rc, lib.gb_last_error_string())
+    return buf.value.decode().split("; ")
+
+
+def test_2d_schedules_without_a_gpu(lib):
+    """2D schedules: one-row row tiles; 4096-row columns as one persistent
+    pass, or -- for real grids at least 4096 wide (c2c: 8192) with the L2
+    hints, and from 8192 rows always -- as a two-pass four-step of 64-column
+    tiles whose intermediates stay in L2 (D: dropped once read)."""
+    rows, c1, c2 = _sched2d(lib, 1, 4096, 4096)
+    assert rows.startswith("tile L=2048 R=16 C=1 ") and "epi=r2c" in rows and rows.endswith("l2=FL")
+    assert "L=64 R=16 C=64" in c1 and "by_row" in c1 and c1.endswith("l2=L")
+    assert "L=64 R=16 C=64" in c2 and c2.endswith("l2=SD")
+    c1, c2, rows = _sched2d(lib, 2, 4096, 4096)
+    assert c1.endswith("l2=FL") and c2.endswith("l2=LD") and "pro=c2r" in rows and rows.endswith("l2=SD")
+    rows, col = _sched2d(lib, 0, 4096, 4096)  # c2c at 4096 wide: one persistent column pass
+    assert col.startswith("tile+persistent L=4096 R=16 C=4")
+    rows, col = _sched2d(lib, 1, 2048, 4096)
+    assert col.startswith("tile+persistent L=4096") and rows.startswith("tile L=1024 R=16 C=1 ")
+    assert len(_sched2d(lib, 1, 4096, 4096, lib.options(columns_2d=1))) == 2
+    assert len(_sched2d(lib, 1, 4096, 4096, lib.options(l2_residency=0))) == 2
+    assert len(_sched2d(lib, 0, 1024, 8192)) == 3
+    buf = C.create_string_buffer(64)
+    assert lib.gb_describe_schedule_2d(1, 3, 4, K.FORWARD, 0, None, buf, 64) == -1
+    lib.gb_clear_error()
+    assert lib.gb_describe_schedule_2d(5, 4, 4, K.FORWARD, 0, None, buf, 64) == -1
+    lib.gb_clear_error()
+
+
 def test_l2_residency_hints_in_schedules(lib):
     """Multi-pass intermediates carry L2 cache-policy hints by default: the
     first pass streams its input and keeps its output (F, L), the last drops
